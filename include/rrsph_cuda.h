@@ -1,0 +1,265 @@
+/*
+ * rrsph_cuda.h — C ABI of the GB300 (sm_103a) WCSPH step.
+ *
+ * This library is a drop-in for the time loop of RRSPH_OMP:
+ *   void time_integration(vheap_darray_floatn& r, vheap_darray_floatn& v,
+ *                         heap_darray<rr_float>& rho, heap_darray<rr_float>& p,
+ *                         heap_darray<rr_int>& itype)
+ *   (sources/RRSPH_OMP/include/TimeIntegration.h:4-9, loop body in
+ *    sources/RRSPH_OMP/src/TimeIntegration.cpp:21-102)
+ * and for the pieces of that loop the reference's own tests call one at a time
+ * (grid_find, density_sum/density_con, the per-pair force terms).
+ *
+ * Conventions
+ *  - Every function returns an int status (RRSPH_OK == 0); nothing throws across
+ *    the ABI. rrsph_last_error() gives a human-readable message for the calling
+ *    thread's last failure.
+ *  - Host vectors (positions, velocities) are particle-major with a caller-given
+ *    stride in doubles: component d of particle i is ptr[i*stride + d]. The
+ *    reference's rr_float2 arrays have stride 2, its padded rr_float3 arrays
+ *    stride 4 (RRSPH_PARAMS/include/RRFloat3.h:5).
+ *  - Particle ids are the row order of the dump CSV, as in the reference.
+ *  - A solver handle owns one CUDA stream and all device buffers. Handles are not
+ *    thread-safe; use one handle per host thread.
+ */
+#ifndef RRSPH_CUDA_H
+#define RRSPH_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RRSPH_ABI_VERSION 1
+
+/* ---- status codes -------------------------------------------------------- */
+enum {
+    RRSPH_OK = 0,
+    RRSPH_ERR_INVALID_ARGUMENT = 1,
+    RRSPH_ERR_CUDA = 2,
+    RRSPH_ERR_OUT_OF_MEMORY = 3,
+    /* "making neighbours grid: error occured" (GridFind.cpp:157-171,184-186) */
+    RRSPH_ERR_NEIGHBOUR_OVERFLOW = 4,
+    /* "cell_idx was >= params.max_cells" (GridFind.cpp:61-72) */
+    RRSPH_ERR_OUT_OF_DOMAIN = 5,
+    /* non-finite r/v/rho/p (ConsistencyCheck.cpp:78-145) */
+    RRSPH_ERR_NON_FINITE = 6,
+    /* particle outside the geometry box (ConsistencyCheck.cpp:162-218) */
+    RRSPH_ERR_OUTSIDE_GEOMETRY = 7,
+    RRSPH_ERR_UNSUPPORTED = 8,
+    RRSPH_ERR_IO = 9,
+    RRSPH_ERR_PARSE = 10,
+    /* "never ending simulation" (UpdateAcceleration.cpp:26-28) */
+    RRSPH_ERR_NEVER_ENDING = 11,
+    RRSPH_ERR_NO_DEVICE = 12
+};
+
+/* Sticky device-side status flags, read with rrsph_status(). */
+#define RRSPH_FLAG_NEIGHBOUR_OVERFLOW 0x1u
+#define RRSPH_FLAG_OUT_OF_DOMAIN      0x2u
+#define RRSPH_FLAG_NON_FINITE         0x4u
+#define RRSPH_FLAG_OUTSIDE_GEOMETRY   0x8u
+#define RRSPH_FLAG_NEVER_ENDING       0x10u
+
+/* Arithmetic of the pair loops.
+ * FP64:  every operation in double, like RRSPH_OMP.
+ * MIXED: pair arithmetic in float32 on cell-relative coordinates with
+ *        Kahan-compensated density and force sums; positions, velocities,
+ *        densities, the integration update and the piston stay in double.
+ *        Cell keys and neighbour sets are identical to FP64 (pairs near the
+ *        cutoff are re-tested in double). */
+enum { RRSPH_PRECISION_FP64 = 0, RRSPH_PRECISION_MIXED = 1 };
+
+/* Force terms for rrsph_forces() (UpdateAcceleration.cpp:66-97). */
+#define RRSPH_TERM_GRAVITY   0x1u  /* a.y = -g start value                       */
+#define RRSPH_TERM_EXTERNAL  0x2u  /* external_force_part  (ExtForce.h:15-60)    */
+#define RRSPH_TERM_INTERNAL  0x4u  /* find_internal_changes_part (InternalForce.h:121-141) */
+#define RRSPH_TERM_ART_VISC  0x8u  /* artificial_viscosity_part (ArtificialViscosity.h:29-65) */
+#define RRSPH_TERM_AVERAGE_VELOCITY 0x10u /* average_velocity_part (AverageVelocity.h:20-37) */
+#define RRSPH_TERM_ALL       0x1Fu /* what update_acceleration sums, per params  */
+
+/* Value of rrsph_params.dt_dynamic_reduce: how DT_CORRECTION_DYNAMIC picks dt.
+ * 0: as the OpenMP build of RRSPH_OMP does — its max reduction is compiled out
+ *    (UpdateAcceleration.cpp:107-121), so update_dt(0, 0) gives dt = CFL*h/c.
+ * 1: the true max of |a| and mu over particles (the serial OMP / CL behaviour). */
+
+/*
+ * Every field of ExperimentParams (sources/RRSPH_PARAMS/include/Params.h:8-196)
+ * that the step reads, plus the derived values fileInput() computes
+ * (sources/RRSPH_COMMON/src/Input.cpp:93-138). Plain old data; all integers are
+ * fixed width. Fill with rrsph_params_defaults(), then from JSON with
+ * rrsph_experiment_load_params(), then rrsph_params_derive().
+ */
+typedef struct rrsph_params {
+    uint32_t struct_size;          /* = sizeof(rrsph_params), set by rrsph_params_defaults */
+    uint32_t dim;                  /* 2 or 3 */
+
+    /* ParticleParams.json */
+    uint64_t ntotal, nfluid, nvirt;
+    double x_mingeom, x_maxgeom, y_mingeom, y_maxgeom, z_mingeom, z_maxgeom;
+    double delta;
+    double rho0;
+    double depth;                  /* 0 => find_depth() from the fluid rows */
+    uint64_t nwm_particles_start, nwm_particles_end;
+
+    /* ModelParams.json */
+    uint32_t density_treatment;    /* 0 summation, 1 continuity, 2 continuity + delta-SPH */
+    uint32_t density_skf;
+    double density_delta_sph_coef;
+    uint32_t eos_sound_vel_method; /* 0 dam break, 1 specific */
+    uint32_t intf_sph_approximation;
+    double eos_sound_vel, eos_sound_vel_coef;
+    double intf_hsml_coef;
+    uint32_t intf_skf;
+    uint32_t artificial_pressure;
+    uint32_t artificial_pressure_skf;
+    uint32_t artificial_viscosity;
+    double artificial_pressure_index, artificial_pressure_coef;
+    double artificial_shear_visc, artificial_bulk_visc;
+    uint32_t artificial_viscosity_skf;
+    uint32_t average_velocity;
+    double average_velocity_coef;
+    uint32_t average_velocity_skf;
+    uint32_t consistency_check;
+    uint32_t consistency_treatment; /* 0 print, 1 stop, 2 fix */
+    uint32_t boundary_treatment;    /* 0 dynamic, 1 repulsive (Lennard-Jones) */
+    uint32_t nwm;                   /* 0 none, 2/3 piston 1st/2nd order, 4 wall disappear, 5 solitary */
+    uint32_t nwm_direction;
+    double nwm_time_start, nwm_wave_length, nwm_wave_magnitude, nwm_phase;
+    double simulation_time;
+    uint32_t dt_correction_method;  /* 0 const value, 1 const CFL, 2 dynamic */
+    uint32_t dt_dynamic_reduce;     /* see above; default 0 */
+    double dt, CFL_coef;
+    uint32_t max_neighbours;
+    uint32_t local_threads;
+    double save_time, dump_time;
+    uint32_t use_dump, save_every_step;
+    uint32_t save_velocity, save_pressure;
+    uint32_t save_density, use_crash_dump;
+    double start_simulation_time;
+
+    /* derived by rrsph_params_derive (Input.cpp:93-138) */
+    double hsml, mass, cell_scale_k;
+    uint64_t maxn, max_cells;
+    double nwm_wave_number, nwm_freq, nwm_piston_magnitude;
+
+    /* constants of ExperimentParams (Params.h:176-193) */
+    double pi, g;
+    int32_t type_boundary, type_non_existent, type_water;
+    uint32_t reserved0;
+} rrsph_params;
+
+typedef struct rrsph_solver rrsph_solver;
+
+/* ---- ABI introspection ---------------------------------------------------- */
+int rrsph_abi_version(void);
+size_t rrsph_params_sizeof(void);
+/* Byte offset of a named rrsph_params field; RRSPH_ERR_INVALID_ARGUMENT if unknown. */
+int rrsph_params_offsetof(const char* field, size_t* offset);
+/* Message for the calling thread's last non-zero status. Never NULL. */
+const char* rrsph_last_error(void);
+
+/* ---- parameters (host only, no GPU needed) -------------------------------- */
+/* Defaults of ExperimentParams + ModelParams + ParticleParams
+ * (Params.h:8-196, ModelParams.h:11-78, ParticleParams.cpp:109-147). */
+int rrsph_params_defaults(rrsph_params* p);
+/* load_particle_params + load_model_params + apply_*_params
+ * (ParticleParams.cpp:51-149, ModelParams.cpp:185-311) from
+ * <dir>/ParticleParams.json and <dir>/ModelParams.json. Mandatory keys and the
+ * reference's "Need optional param"/"Not implemented" checks are enforced. */
+int rrsph_experiment_load_params(const char* experiment_dir, rrsph_params* p);
+/* fillInComputingParams + find_depth + postFillInModelParams
+ * (Input.cpp:17-138, 238-331). r holds the ntotal loaded positions. */
+int rrsph_params_derive(rrsph_params* p, const double* r, uint32_t stride);
+/* Start time taken from a dump file name stem, as Input.cpp:258 (std::stod). */
+int rrsph_layer_time_from_path(const char* path, double* t);
+
+/* ---- particle layers (CSV; host only) ------------------------------------- */
+/* loadArrays (Input.cpp:203-236): columns x,y[,z],itype,vx,vy[,vz],rho by name;
+ * p is read if present. Row count must equal p->ntotal. */
+int rrsph_layer_read(const char* csv_path, const rrsph_params* p,
+                     double* r, uint32_t stride, double* v, double* rho,
+                     double* pres, int32_t* itype);
+/* print_dump / print (Output.cpp:118-221): std::to_string formatting (6
+ * decimals). dump != 0 writes every column; otherwise the save_* switches
+ * choose v, rho, p. */
+int rrsph_layer_write(const char* csv_path, const rrsph_params* p,
+                      const double* r, uint32_t stride, const double* v,
+                      const double* rho, const double* pres,
+                      const int32_t* itype, int dump);
+
+/* ---- solver --------------------------------------------------------------- */
+/* Allocates device buffers for p->ntotal particles on the current CUDA device.
+ * p must be derived. precision: RRSPH_PRECISION_FP64 or RRSPH_PRECISION_MIXED. */
+int rrsph_create(const rrsph_params* p, int precision, rrsph_solver** out);
+void rrsph_destroy(rrsph_solver* s);
+/* The handle's CUDA stream (a cudaStream_t), for callers that order their own
+ * work after the solver's. */
+int rrsph_get_stream(rrsph_solver* s, void** stream);
+
+/* Host -> device copy of the whole state (ntotal rows). Resets the step
+ * counter, the accelerations and drho to zero, as time_integration() starts
+ * with fresh work arrays (TimeIntegration.cpp:35-50). pres may be NULL. */
+int rrsph_upload(rrsph_solver* s, const double* r, uint32_t stride,
+                 const double* v, const double* rho, const double* pres,
+                 const int32_t* itype);
+/* Device -> host copy of the state; any pointer may be NULL to skip it. */
+int rrsph_download(rrsph_solver* s, double* r, uint32_t stride, double* v,
+                   double* rho, double* pres, int32_t* itype);
+
+/* nsteps iterations of the time loop body (TimeIntegration.cpp:60-100):
+ * predict_half_step, grid_find, density, update_acceleration, piston
+ * (when nwm is a piston and time >= nwm_time_start), whole_step, time += dt.
+ * *time_io is the simulation time before the first step and is advanced.
+ * The first step after rrsph_upload uses dt/2 for velocities (WholeStep.cpp:33). */
+int rrsph_step(rrsph_solver* s, uint64_t nsteps, double* time_io);
+/* Sticky RRSPH_FLAG_* bits raised by device checks since the last clear. */
+int rrsph_status(rrsph_solver* s, uint32_t* flags, int clear);
+/* Current time step (changes under DT_CORRECTION_DYNAMIC with dt_dynamic_reduce). */
+int rrsph_get_dt(rrsph_solver* s, double* dt);
+
+/* ---- loop pieces, on the uploaded state (the reference's unit-test path) ---- */
+/* make_grid (GridFind.cpp:47-88): keys[i] = Morton cell index of particle i
+ * (get_cell_idx2/3, GridUtils.h:135-150); grid = particle ids sorted by
+ * (cell, id); cells_start (max_cells+1 entries, may be NULL) = index of the
+ * first grid entry of each cell, as after the reference's reverse scatter. */
+int rrsph_grid_find(rrsph_solver* s, uint32_t* keys, uint32_t* grid,
+                    uint32_t* cells_start);
+/* find_neighbours (GridFind.cpp:112-189): counts[j] = number of neighbours of
+ * particle j, list[j*max_per + n] = n-th neighbour in the reference's order
+ * (3^dim cells x-major, ids ascending within a cell). Needs
+ * counts[j] <= max_per; otherwise RRSPH_ERR_NEIGHBOUR_OVERFLOW. */
+int rrsph_neighbours(rrsph_solver* s, uint32_t* counts, uint32_t* list,
+                     uint32_t max_per, uint64_t* total_pairs);
+/* density_sum (Density.h:25-61) or density_con (Density.h:63-114) by
+ * density_treatment, on r, v, rho of the uploaded state. Writes rho (summation)
+ * or drho (continuity) into out_rho_or_drho and p into out_p, and stores rho/p
+ * in the device state as the loop does. */
+int rrsph_density(rrsph_solver* s, double* out_rho_or_drho, double* out_p);
+/* Sum over neighbours of the selected terms (RRSPH_TERM_*), on r, v, rho, p of
+ * the device state: a[j] (stride `stride`), av[j] (XSPH, may be NULL), mu[j] =
+ * max |mu_ij| of the artificial viscosity (may be NULL). Terms also need their
+ * params switch on (artificial_viscosity, average_velocity, boundary_treatment). */
+int rrsph_forces(rrsph_solver* s, uint32_t terms, double* a, uint32_t stride,
+                 double* av, double* mu);
+
+/* ---- timing hooks for benchmarks ------------------------------------------ */
+/* Number of kernel phases one step launches and their names. */
+int rrsph_phase_count(rrsph_solver* s, int* count);
+const char* rrsph_phase_name(rrsph_solver* s, int phase);
+/* When enabled, rrsph_step records CUDA events around every phase; the
+ * accumulated milliseconds per phase (since the last reset) and the number of
+ * steps are returned by rrsph_phase_times. Enabling it disables graph replay. */
+int rrsph_set_phase_timing(rrsph_solver* s, int enable);
+int rrsph_phase_times(rrsph_solver* s, double* ms_per_phase, int count,
+                      uint64_t* steps, int reset);
+/* Launches of the library's own kernels since creation (all phases). */
+int rrsph_kernel_launches(rrsph_solver* s, uint64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RRSPH_CUDA_H */

@@ -1,0 +1,46 @@
+#!/bin/sh
+# Builds the reference's own RRSPH_OMP compute core from its sources, in place,
+# together with oracle/ref_driver.cpp, into oracle/_ref/rrsph_ref (TEST
+# INFRASTRUCTURE: used to pin the C oracle and as the "reference" CPU baseline
+# where the reference sources exist). Outputs go to oracle/_ref/ only.
+#
+# Only the compute core builds here: the reference's executable needs fmt and
+# googletest, which it does not vendor. Two things are generated into
+# oracle/_ref/gen/ instead of edited in the reference tree:
+#   - the version headers, from the reference's *.h.in templates (CMake
+#     configure_file values of CMakeLists.txt: RRSPH 3.1.4, RRSPH_COMMON 1.3.4,
+#     RRSPH_OMP 1.4.1);
+#   - a copy of Params.h, Types.h and RRFloatnDArray.h in which the MSVC-only
+#     `throw std::exception{"..."}` of RRFloatnDArray.h becomes
+#     `throw std::runtime_error{"..."}` so that GCC accepts it (the other two are
+#     copied so that their quoted includes resolve to the patched header).
+set -eu
+REF="${RRSPH_REFERENCE:-/root/reference}"
+HERE="$(cd "$(dirname "$0")" && pwd)"
+OUT="$HERE/_ref"
+S="$REF/sources"
+if [ ! -d "$S/RRSPH_OMP/src" ]; then
+    echo "build_ref: reference sources not found under $REF; nothing built"
+    exit 0
+fi
+mkdir -p "$OUT/gen"
+ver() { sed "s/@PROJECT_VERSION_MAJOR@/$2/;s/@PROJECT_VERSION_MINOR@/$3/;s/@PROJECT_VERSION_PATCH@/$4/" "$1"; }
+ver "$S/RRSPH_PARAMS/ParamsVersion.h.in" 3 1 4 > "$OUT/gen/ParamsVersion.h"
+ver "$S/RRSPHVersion.h.in" 3 1 4 > "$OUT/gen/RRSPHVersion.h"
+ver "$S/RRSPH_COMMON/RRSPHCOMMONVersion.h.in" 1 3 4 > "$OUT/gen/RRSPHCOMMONVersion.h"
+ver "$S/RRSPH_OMP/RRSPHOMPVersion.h.in" 1 4 1 > "$OUT/gen/RRSPHOMPVersion.h"
+cp "$S/RRSPH_PARAMS/include/Params.h" "$S/RRSPH_PARAMS/include/Types.h" "$OUT/gen/"
+sed -e 's/std::exception{/std::runtime_error{/' -e 's/#include <variant>/#include <variant>\n#include <stdexcept>/' \
+    "$S/RRSPH_PARAMS/include/RRFloatnDArray.h" > "$OUT/gen/RRFloatnDArray.h"
+chmod u+w "$OUT/gen/"*
+
+CXX="${CXX:-g++}"
+"$CXX" -std=c++20 -O2 -fopenmp -ffp-contract=off -w \
+    -DRRSPH_OMP -DDO_ON_CPU=1 -DDO_ON_GPU=0 -DLOGGING_LEVEL=0 \
+    -I"$OUT/gen" -I"$S/RRSPH_PARAMS/include" -I"$S/RRSPH_COMMON/include" \
+    -I"$S/RRSPH_OMP/include" -I"$S/RR/include" \
+    "$S/RRSPH_OMP/src/GridFind.cpp" "$S/RRSPH_OMP/src/UpdateAcceleration.cpp" \
+    "$S/RRSPH_OMP/src/PredictHalfStep.cpp" "$S/RRSPH_OMP/src/WholeStep.cpp" \
+    "$S/RRSPH_OMP/src/WaveMaker.cpp" "$S/RRSPH_COMMON/src/EOS.cpp" \
+    "$HERE/ref_driver.cpp" -o "$OUT/rrsph_ref"
+echo "build_ref: built $OUT/rrsph_ref"

@@ -1,0 +1,178 @@
+// common.cuh — device-side definitions shared by the WCSPH kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/rrsph_cuda.h"
+
+namespace rrsph {
+
+constexpr uint32_t kInvalidCell = 0xFFFFFFFFu;      // GRID_INVALID_CELL (GridUtils.h:8)
+constexpr uint32_t kMaxCellCoord2 = (1u << 16) - 1; // GRID_MAX_CELL_COORD2 (GridUtils.h:9)
+constexpr uint32_t kEmpty = 0xFFFFFFFFu;            // empty cell-table entry
+
+// Everything a kernel needs from rrsph_params, precomputed on the host.
+struct DevParams {
+    int dim;
+    uint32_t n;             // ntotal
+    uint32_t nfluid;
+    uint32_t max_cells;     // Morton key bound (power of two)
+    uint32_t max_nb;        // max_neighbours: the reference stores at most max_nb - 1
+    int type_non_existent;
+    double xmin, ymin, zmin, xmax, ymax, zmax;
+    double cell;            // cell_scale_k * hsml (grid_cell_size)
+    double inv_cell;
+    double cut2;            // sqr(grid_cell_size()) computed as the reference does
+    double h, inv_h, mass, g, rho0;
+    double B;               // EOS: c^2 rho0 / 7
+    double c_eos;           // eos_art_c()
+    double c_av;            // params.eos_sound_vel used by the artificial viscosity
+    double etq_h2;          // sqr(hsml * 0.1f)
+    double w0_density;      // smoothing_kernel_w(0, density_skf)
+    double kf[5];           // kernel factors by skf (index 1..4)
+    int density_skf, intf_skf, av_skf, avel_skf, ap_skf;
+    int density_treatment;  // 0 sum, 1 con, 2 con + delta
+    double delta_sph_dhc;   // density_delta_sph_coef * hsml * eos_art_c()
+    int intf_form;          // 1 or 2
+    int art_pressure;
+    double ap_index, ap_coef, ap_wdelta;  // wdelta = smoothing_kernel_w(delta, ap_skf)
+    int art_visc;
+    double av_alpha, av_beta;
+    int avg_vel;
+    double avg_vel_coef;
+    int repulsive;          // boundary_treatment == SBT_REPULSIVE
+    double lj_rr0, lj_D;
+    int consistency_check, consistency_treatment;
+    // piston / wave maker
+    int nwm;
+    uint32_t nwm_start, nwm_end;
+    int nwm_valid;
+    double nwm_time_start, nwm_phase, nwm_freq, nwm_H, nwm_k, depth;
+    // dt control
+    int dt_method;          // 0 const, 1 CFL const, 2 dynamic
+    int dt_reduce;          // 1: true max reduction
+    double cfl, never_ending_dt;
+};
+
+// Per-step scalars kept on the device (double-buffered by step parity so a
+// captured step graph can advance them without host involvement).
+struct StepScalars {
+    double time;
+    double dt;
+    unsigned long long step;   // itimestep of the reference loop
+    unsigned long long amax_bits;  // max |a| over particles (as ordered bits)
+    unsigned long long mumax_bits; // max arvmu
+    unsigned long long pairs;      // directed pairs found by the density gather
+    unsigned long long pad[2];
+};
+
+// ---------------------------------------------------------------- Morton --
+// GridUtils.h:50-64 and 92-104, computed in 64-bit like rr_uint.
+__host__ __device__ inline uint64_t split2(uint64_t x) {
+    x = (x | x << 16) & 0x0000FFFFull;
+    x = (x | x << 8) & 0x00FF00FFull;
+    x = (x | x << 4) & 0x0F0F0F0Full;
+    x = (x | x << 2) & 0x33333333ull;
+    x = (x | x << 1) & 0x55555555ull;
+    return x;
+}
+__host__ __device__ inline uint64_t split3(uint64_t a) {
+    uint64_t x = a & 0x000003ffull;
+    x = (x | x << 16) & 0x30000ffull;
+    x = (x | x << 8) & 0x0300f00full;
+    x = (x | x << 4) & 0x30c30c3ull;
+    x = (x | x << 2) & 0x9249249ull;
+    return x;
+}
+__host__ __device__ inline uint32_t second_bits(uint32_t m) { // GridUtils.h:107-114
+    uint32_t x = m & 0x55555555u;
+    x = (x ^ (x >> 1)) & 0x33333333u;
+    x = (x ^ (x >> 2)) & 0x0F0F0F0Fu;
+    x = (x ^ (x >> 4)) & 0x00FF00FFu;
+    x = (x ^ (x >> 8)) & 0x0000FFFFu;
+    return x;
+}
+__host__ __device__ inline uint32_t third_bits(uint32_t m) { // GridUtils.h:67-74
+    uint32_t x = m & 0x9249249u;
+    x = (x ^ (x >> 2)) & 0x30c30c3u;
+    x = (x ^ (x >> 4)) & 0x0300f00fu;
+    x = (x ^ (x >> 8)) & 0x30000ffu;
+    x = (x ^ (x >> 16)) & 0x000003ffu;
+    return x;
+}
+
+// get_cell_coord_from_particle_coord (GridUtils.h:135-137): truncation of
+// (r - r_min) / cell. A negative quotient (outside the geometry) maps to 0 and
+// is reported through the out-of-domain flag by the key pass.
+__device__ inline uint64_t cell_coord(double r, double rmin, double cell) {
+    const double c = __ddiv_rn(__dsub_rn(r, rmin), cell);
+    if (!(c >= 0.0)) return 0;
+    if (c >= 18446744073709551615.0) return ~0ull;
+    return (uint64_t)c;
+}
+
+// Neighbour-cell coordinate steps (GridUtils.h:158-163).
+__device__ inline uint64_t step_coord(uint64_t c, int d) {
+    if (d < 0) return c == 0 ? (uint64_t)kInvalidCell : c - 1;
+    if (d > 0) return c == kMaxCellCoord2 ? (uint64_t)kInvalidCell : c + 1;
+    return c;
+}
+
+// ------------------------------------------------------ smoothing kernels --
+// SmoothingKernel.h:20-274 with q = dist * (1/h). `f` is the factor of skf.
+__device__ inline double kernel_w(int skf, double f, double q) {
+    switch (skf) {
+    case 2: return f * exp(-q * q);
+    case 3: {
+        if (q <= 2.0) {
+            const double t = 1.0 - 0.5 * q;
+            const double t2 = t * t;
+            return f * (t2 * t2) * (2.0 * q + 1.0);
+        }
+        return 0.0;
+    }
+    case 4: {
+        if (q <= 2.0) { const double t = 2.0 - q; return f * (t * t * t); }
+        return 0.0;
+    }
+    default:
+        if (q <= 1.0) return f * (2.0 / 3.0 - q * q + q * q * q * 0.5);
+        if (q <= 2.0) { const double t = 2.0 - q; return f * (1.0 / 6.0 * (t * t * t)); }
+        return 0.0;
+    }
+}
+
+// Scalar s such that dW/dr = diff * s (diff = r_i - r_j, |diff| = dist).
+__device__ inline double kernel_dwdr_scale(int skf, double f, double q, double dist, double inv_h) {
+    switch (skf) {
+    case 2: return inv_h * inv_h * (-2.0) * (f * exp(-q * q));
+    case 3: {
+        if (q < (double)1.e-6f || !(q < 2.0)) return 0.0;
+        const double t = 1.0 - 0.5 * q;
+        const double t3 = t * t * t;
+        return inv_h / dist * f * 2.0 * (t3 * t - (2.0 * q + 1.0) * t3);
+    }
+    case 4: {
+        if (q < 2.0) { const double t = 2.0 - q; return inv_h / dist * f * (-3.0 * t * t); }
+        return 0.0;
+    }
+    default:
+        if (q <= 1.0) return inv_h * inv_h * f * (-2.0 + 1.5 * q);
+        if (q <= 2.0) { const double t = 2.0 - q; return -(inv_h / dist) * f * (t * t * 0.5); }
+        return 0.0;
+    }
+}
+
+// eos_art_p (EOS.cpp:31-34)
+__device__ inline double eos_p(const DevParams& P, double rho) {
+    const double x = rho / P.rho0;
+    const double x2 = x * x;
+    const double x4 = x2 * x2;
+    return P.B * (x4 * x2 * x - 1.0);
+}
+
+// Ordered-bits encoding of non-negative doubles for atomicMax.
+__device__ inline unsigned long long dbits(double v) { return (unsigned long long)__double_as_longlong(v); }
+
+}  // namespace rrsph

@@ -1,0 +1,85 @@
+// kernels.cuh — device buffers of a solver and the launchers of its kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace rrsph {
+
+// Particle state in id order (the reference's arrays), double precision.
+struct State {
+    double *rx, *ry, *rz;      // positions
+    double *vx, *vy, *vz;      // velocities
+    double *ax, *ay, *az;      // accelerations of the last force evaluation
+    double *avx, *avy, *avz;   // XSPH average velocity (average_velocity only)
+    double *vpx, *vpy, *vpz;   // v_predict
+    double *rho, *p, *drho, *rho_pred;
+    double *mu;                // max |mu_ij| per particle (rrsph_forces only)
+    int32_t* itype;
+    uint32_t* key_of;          // cell key used by the last grid build, per id
+};
+
+// Per-step cell-ordered copies and the grid.
+struct Sorted {
+    uint32_t *keys_in, *ids_in;       // key pass output (id order)
+    uint32_t *keys_a, *ids_a, *keys_b, *ids_b;
+    uint32_t* sort_scratch;
+    uint32_t *key, *id;               // sorted result (points into a or b)
+    uint32_t *cell_start, *cell_end;  // [max_cells]
+    // FP64 gathers
+    double *rx, *ry, *rz;
+    double *vx, *vy, *vz;             // velocity the forces use (v_predict in the loop)
+    double *vdx, *vdy, *vdz;          // velocity of density_con (v)
+    double *rho;                      // density the forces use
+    double *rhod;                     // density of density_con
+    double* p;
+    int32_t* itype;
+    // FP32-mixed gathers
+    float4* P4;    // cell-relative position (x, y, z) + itype bits
+    float4* V4;    // velocity the forces use + density the forces use
+    float4* VD4;   // v + rho for density_con
+    float* pf;     // pressure
+};
+
+// Sources the reorder gathers for the force velocity / density.
+struct GatherSrc {
+    const double *vx, *vy, *vz;
+    const double* rho;
+    const double* p;  // pressure to copy (rrsph_forces on the given state); null in the loop
+};
+
+template <int DIM>
+void launch_keys(const DevParams& P, const State& S, Sorted& G, StepScalars* scal, int predict, uint32_t* flags,
+                 cudaStream_t st);
+template <int DIM>
+void launch_reorder(const DevParams& P, const State& S, const Sorted& G, GatherSrc fsrc, int mixed, cudaStream_t st);
+template <int DIM>
+void launch_density_fp64(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
+                         cudaStream_t st);
+template <int DIM>
+void launch_forces_fp64(const DevParams& P, const State& S, const Sorted& G, uint32_t terms, StepScalars* scal,
+                        uint32_t* flags, int write_mu, cudaStream_t st);
+template <int DIM>
+void launch_density_mixed(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
+                          cudaStream_t st);
+template <int DIM>
+void launch_forces_mixed(const DevParams& P, const State& S, const Sorted& G, uint32_t terms, StepScalars* scal,
+                         uint32_t* flags, int write_mu, cudaStream_t st);
+template <int DIM>
+void launch_whole_step(const DevParams& P, const State& S, StepScalars* scal_cur, StepScalars* scal_next,
+                       uint32_t* flags, cudaStream_t st);
+
+void launch_cells_start(const DevParams& P, const Sorted& G, uint32_t* out, cudaStream_t st);
+template <int DIM>
+void launch_neighbour_list(const DevParams& P, const Sorted& G, uint32_t* counts, uint32_t* list, uint32_t max_per,
+                           uint32_t* flags, cudaStream_t st);
+template <int DIM>
+void launch_unpack(const DevParams& P, State S, const double* r, const double* v, uint32_t stride, cudaStream_t st);
+template <int DIM>
+void launch_pack(const DevParams& P, State S, double* r, double* v, uint32_t stride, cudaStream_t st);
+
+constexpr int kGatherThreads = 128;
+
+}  // namespace rrsph

@@ -1,0 +1,650 @@
+// solver.cu — the C ABI of the GPU step: solver handles, upload/download,
+// the captured step graphs and the loop-piece entry points.
+//
+// One step is the loop body of time_integration
+// (sources/RRSPH_OMP/src/TimeIntegration.cpp:60-100):
+//   keys      predict_half_step + cell keys      (PredictHalfStep.cpp:4-23, GridFind.cpp:55-75)
+//   sort      stable radix sort by (cell, id)    (GridFind.cpp:53-87)
+//   reorder   cell-order copies + cell table     (GridFind.cpp:77-87)
+//   density   density_sum | density_con          (Density.h:25-114)
+//   forces    update_acceleration                (UpdateAcceleration.cpp:33-125)
+//   whole     piston + whole_step + bounds check (WaveMaker.cpp:34-82, WholeStep.cpp:19-62)
+// The sequence is captured once per step parity into a CUDA graph and replayed;
+// the scalars that change between steps (time, dt, step counter) live on the
+// device, double-buffered by parity, and are advanced by the whole-step kernel.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../host/error.hpp"
+#include "kernels.cuh"
+#include "sort.cuh"
+
+using rrsph::set_error;
+
+namespace {
+
+constexpr int kPhases = 6;
+const char* const kPhaseNames[kPhases] = {"keys", "sort", "reorder", "density", "forces", "whole"};
+constexpr uint32_t kFlagNeverEnding = RRSPH_FLAG_NEVER_ENDING;
+
+}  // namespace
+
+struct rrsph_solver {
+    rrsph_params params{};
+    rrsph::DevParams P{};
+    int precision = RRSPH_PRECISION_FP64;
+    int dim = 2;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    rrsph::State S{};
+    rrsph::Sorted G{};
+    rrsph::StepScalars* scal = nullptr;  // [2] on the device
+    uint32_t* flags = nullptr;
+    rrsph::StepScalars* h_scal = nullptr;  // pinned
+    uint32_t* h_flags = nullptr;           // pinned
+    double* h_time = nullptr;              // pinned
+    double* staging = nullptr;
+    size_t staging_words = 0;
+    std::vector<void*> allocations;
+    int sort_bits = 0;
+    bool graphs = true;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    unsigned long long launches = 0;
+    unsigned long long launches_in_graph[2] = {0, 0};
+    uint64_t step_index = 0;
+    bool timing = false;
+    cudaEvent_t ev[kPhases + 1] = {};
+    double phase_ms[kPhases] = {};
+    uint64_t timed_steps = 0;
+};
+
+namespace {
+
+#define RRSPH_CUDA_TRY(call)                                                                       \
+    do {                                                                                           \
+        cudaError_t err_ = (call);                                                                 \
+        if (err_ != cudaSuccess)                                                                   \
+            return set_error(err_ == cudaErrorMemoryAllocation ? RRSPH_ERR_OUT_OF_MEMORY : RRSPH_ERR_CUDA, \
+                             std::string(#call) + ": " + cudaGetErrorString(err_));                \
+    } while (0)
+
+template <typename T>
+int dev_alloc(rrsph_solver* s, T** ptr, size_t count) {
+    *ptr = nullptr;
+    if (count == 0) return RRSPH_OK;
+    void* p = nullptr;
+    RRSPH_CUDA_TRY(cudaMalloc(&p, count * sizeof(T)));
+    s->allocations.push_back(p);
+    *ptr = static_cast<T*>(p);
+    return RRSPH_OK;
+}
+
+// Host copies of the smoothing-kernel factors and W (SmoothingKernel.h).
+double host_factor(const rrsph_params& p, int skf) {
+    const double h = p.hsml, pi = p.pi;
+    const bool d3 = p.dim == 3;
+    switch (skf) {
+    case 2: return d3 ? 1 / (pi * std::sqrt(pi) * h * h * h) : 1 / (pi * (h * h));
+    case 3: return d3 ? 21 / (16 * pi * (h * h * h)) : 7 / (4 * pi * (h * h));
+    case 4: return d3 ? 15 / (pi * ((4 * h) * (4 * h) * (4 * h))) : 5 / (16 * pi * (h * h));
+    default: return d3 ? 3.0 / (2.0 * pi * (h * h * h)) : 15.0 / (7.0 * pi * (h * h));
+    }
+}
+double host_w(const rrsph_params& p, double dist, int skf) {
+    const double q = dist / p.hsml, f = host_factor(p, skf);
+    switch (skf) {
+    case 2: return f * std::exp(-q * q);
+    case 3: { if (q <= 2) { const double t = 1 - 0.5 * q; return f * t * t * t * t * (2 * q + 1); } return 0; }
+    case 4: { if (q <= 2) { const double t = 2 - q; return f * t * t * t; } return 0; }
+    default:
+        if (q <= 1) return f * (2.0 / 3.0 - q * q + q * q * q * 0.5);
+        if (q <= 2) { const double t = 2.0 - q; return f * (1.0 / 6.0 * (t * t * t)); }
+        return 0;
+    }
+}
+
+int fill_dev_params(const rrsph_params& p, rrsph::DevParams& P) {
+    std::memset(&P, 0, sizeof(P));
+    P.dim = (int)p.dim;
+    P.n = (uint32_t)p.ntotal;
+    P.nfluid = (uint32_t)p.nfluid;
+    if (p.max_cells == 0 || p.max_cells > (1ull << 32))
+        return set_error(RRSPH_ERR_UNSUPPORTED, "max_cells out of range; derive the params first");
+    P.max_cells = (uint32_t)std::min<uint64_t>(p.max_cells, 0xFFFFFFFFull);
+    P.max_nb = p.max_neighbours;
+    P.type_non_existent = p.type_non_existent;
+    P.xmin = p.x_mingeom; P.ymin = p.y_mingeom; P.zmin = p.z_mingeom;
+    P.xmax = p.x_maxgeom; P.ymax = p.y_maxgeom; P.zmax = p.z_maxgeom;
+    P.cell = p.cell_scale_k * p.hsml;
+    P.inv_cell = 1.0 / P.cell;
+    P.cut2 = P.cell * P.cell;
+    P.h = p.hsml;
+    P.inv_h = 1.0 / p.hsml;
+    P.mass = p.mass;
+    P.g = p.g;
+    P.rho0 = p.rho0;
+    const double c_sqr = p.eos_sound_vel_method == 0 ? 200 * p.g * p.depth * p.eos_sound_vel_coef : p.eos_sound_vel;
+    P.c_eos = std::sqrt(c_sqr);
+    P.B = c_sqr * p.rho0 / 7;
+    P.c_av = p.eos_sound_vel;
+    P.etq_h2 = (p.hsml * (double)0.1f) * (p.hsml * (double)0.1f);
+    for (int s = 1; s <= 4; s++) P.kf[s] = host_factor(p, s);
+    P.kf[0] = P.kf[1];
+    auto skf = [](uint32_t v) { return (v >= 1 && v <= 4) ? (int)v : 1; };
+    P.density_skf = skf(p.density_skf);
+    P.intf_skf = skf(p.intf_skf);
+    P.av_skf = skf(p.artificial_viscosity_skf);
+    P.avel_skf = skf(p.average_velocity_skf);
+    P.ap_skf = skf(p.artificial_pressure_skf);
+    P.w0_density = host_w(p, 0, P.density_skf);
+    P.density_treatment = (int)p.density_treatment;
+    P.delta_sph_dhc = p.density_delta_sph_coef * p.hsml * P.c_eos;
+    P.intf_form = p.intf_sph_approximation == 1 ? 1 : 2;
+    P.art_pressure = p.artificial_pressure ? 1 : 0;
+    P.ap_index = p.artificial_pressure_index;
+    P.ap_coef = p.artificial_pressure_coef;
+    P.ap_wdelta = host_w(p, p.delta, P.ap_skf);
+    P.art_visc = p.artificial_viscosity ? 1 : 0;
+    P.av_alpha = p.artificial_shear_visc;
+    P.av_beta = p.artificial_bulk_visc;
+    P.avg_vel = p.average_velocity ? 1 : 0;
+    P.avg_vel_coef = p.average_velocity_coef;
+    P.repulsive = p.boundary_treatment == 1;
+    P.lj_rr0 = 2 * p.hsml;
+    P.lj_D = 5 * p.g * p.depth;
+    P.consistency_check = p.consistency_check ? 1 : 0;
+    P.consistency_treatment = (int)p.consistency_treatment;
+    P.nwm = (int)p.nwm;
+    P.nwm_start = (uint32_t)std::min<uint64_t>(p.nwm_particles_start, 0xFFFFFFFFull);
+    P.nwm_end = (uint32_t)std::min<uint64_t>(p.nwm_particles_end, 0xFFFFFFFFull);
+    P.nwm_valid = !(p.nwm_particles_start < p.nfluid || p.nwm_particles_end < p.nfluid ||
+                    p.nwm_particles_end < p.nwm_particles_start || p.nwm_particles_end > p.ntotal);
+    P.nwm_time_start = p.nwm_time_start;
+    P.nwm_phase = p.nwm_phase;
+    P.nwm_freq = p.nwm_freq;
+    P.nwm_H = p.nwm_wave_magnitude;
+    P.nwm_k = p.nwm_wave_number;
+    P.depth = p.depth;
+    P.dt_method = (int)p.dt_correction_method;
+    P.dt_reduce = p.dt_dynamic_reduce ? 1 : 0;
+    P.cfl = p.CFL_coef;
+    P.never_ending_dt = (p.hsml / P.c_eos) * 1.E-6;
+    return RRSPH_OK;
+}
+
+int key_bits(uint64_t max_cells) {
+    int b = 0;
+    while ((1ull << b) < max_cells) b++;
+    return b < 1 ? 1 : b;
+}
+
+int check_handle(rrsph_solver* s, const char* fn) {
+    if (!s) return set_error(RRSPH_ERR_INVALID_ARGUMENT, std::string(fn) + ": null solver");
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return set_error(RRSPH_ERR_CUDA, std::string(fn) + ": cudaSetDevice: " + cudaGetErrorString(e));
+    return RRSPH_OK;
+}
+
+// Builds the grid on the current state: keys (optionally with the predictor),
+// sort, reorder with the given force-side sources.
+template <int DIM>
+void enqueue_grid(rrsph_solver* s, int predict, rrsph::StepScalars* scal, rrsph::GatherSrc fsrc) {
+    rrsph::launch_keys<DIM>(s->P, s->S, s->G, scal, predict, s->flags, s->stream);
+    rrsph::radix_sort_pairs(s->G.keys_in, s->G.ids_in, s->G.keys_a, s->G.ids_a, s->G.sort_scratch, s->P.n,
+                            s->sort_bits, s->stream, &s->G.key, &s->G.id, &s->launches);
+    rrsph::launch_reorder<DIM>(s->P, s->S, s->G, fsrc, s->precision == RRSPH_PRECISION_MIXED, s->stream);
+    s->launches += 2;
+}
+
+template <int DIM>
+void enqueue_density(rrsph_solver* s, rrsph::StepScalars* scal) {
+    if (s->precision == RRSPH_PRECISION_MIXED) rrsph::launch_density_mixed<DIM>(s->P, s->S, s->G, scal, s->flags, s->stream);
+    else rrsph::launch_density_fp64<DIM>(s->P, s->S, s->G, scal, s->flags, s->stream);
+    s->launches++;
+}
+
+template <int DIM>
+void enqueue_forces(rrsph_solver* s, uint32_t terms, rrsph::StepScalars* scal, int write_mu) {
+    if (s->precision == RRSPH_PRECISION_MIXED)
+        rrsph::launch_forces_mixed<DIM>(s->P, s->S, s->G, terms, scal, s->flags, write_mu, s->stream);
+    else rrsph::launch_forces_fp64<DIM>(s->P, s->S, s->G, terms, scal, s->flags, write_mu, s->stream);
+    s->launches++;
+}
+
+// One loop step on parity `par`; events[i] (if non-null) are recorded between phases.
+template <int DIM>
+void enqueue_step(rrsph_solver* s, int par, cudaEvent_t* events) {
+    rrsph::StepScalars* cur = s->scal + par;
+    rrsph::StepScalars* nxt = s->scal + (par ^ 1);
+    const bool cont = s->P.density_treatment != 0;
+    rrsph::GatherSrc fsrc{s->S.vpx, s->S.vpy, s->S.vpz, cont ? s->S.rho_pred : s->S.rho, nullptr};
+    if (events) cudaEventRecord(events[0], s->stream);
+    rrsph::launch_keys<DIM>(s->P, s->S, s->G, cur, 1, s->flags, s->stream);
+    if (events) cudaEventRecord(events[1], s->stream);
+    rrsph::radix_sort_pairs(s->G.keys_in, s->G.ids_in, s->G.keys_a, s->G.ids_a, s->G.sort_scratch, s->P.n,
+                            s->sort_bits, s->stream, &s->G.key, &s->G.id, &s->launches);
+    if (events) cudaEventRecord(events[2], s->stream);
+    rrsph::launch_reorder<DIM>(s->P, s->S, s->G, fsrc, s->precision == RRSPH_PRECISION_MIXED, s->stream);
+    if (events) cudaEventRecord(events[3], s->stream);
+    enqueue_density<DIM>(s, cur);
+    if (events) cudaEventRecord(events[4], s->stream);
+    enqueue_forces<DIM>(s, RRSPH_TERM_ALL, cur, 0);
+    if (events) cudaEventRecord(events[5], s->stream);
+    rrsph::launch_whole_step<DIM>(s->P, s->S, cur, nxt, s->flags, s->stream);
+    if (events) cudaEventRecord(events[6], s->stream);
+    s->launches += 3;
+}
+
+void enqueue_step_dim(rrsph_solver* s, int par, cudaEvent_t* events) {
+    if (s->dim == 3) enqueue_step<3>(s, par, events);
+    else enqueue_step<2>(s, par, events);
+}
+
+int ensure_staging(rrsph_solver* s, size_t words) {
+    if (s->staging_words >= words) return RRSPH_OK;
+    if (s->staging) {
+        cudaFree(s->staging);
+        for (auto& a : s->allocations)
+            if (a == s->staging) a = nullptr;
+        s->staging = nullptr;
+    }
+    int rc = dev_alloc(s, &s->staging, words);
+    if (rc) return rc;
+    s->staging_words = words;
+    return RRSPH_OK;
+}
+
+int flags_to_status(const rrsph_solver* s, uint32_t f) {
+    if (f & RRSPH_FLAG_OUT_OF_DOMAIN) return set_error(RRSPH_ERR_OUT_OF_DOMAIN, "cell_idx was >= params.max_cells");
+    if (f & RRSPH_FLAG_NEIGHBOUR_OVERFLOW) return set_error(RRSPH_ERR_NEIGHBOUR_OVERFLOW, "making neighbours grid: error occured");
+    if (f & kFlagNeverEnding) return set_error(RRSPH_ERR_NEVER_ENDING, "never ending simulation");
+    if ((f & RRSPH_FLAG_OUTSIDE_GEOMETRY) && s->params.consistency_check && s->params.consistency_treatment == 1)
+        return set_error(RRSPH_ERR_OUTSIDE_GEOMETRY, "Encounter particle outside boundaries");
+    return RRSPH_OK;
+}
+
+}  // namespace
+
+// ============================================================== C ABI ======
+
+extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver** out) {
+    if (!p || !out) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_create: null argument");
+    *out = nullptr;
+    if (p->struct_size != sizeof(rrsph_params))
+        return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_create: params not initialised by rrsph_params_defaults");
+    if (p->dim != 2 && p->dim != 3) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_create: dim must be 2 or 3");
+    if (p->ntotal == 0 || p->ntotal >= (1ull << 31)) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_create: bad ntotal");
+    if (p->hsml <= 0 || p->mass <= 0) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_create: derive the params first");
+    if (precision != RRSPH_PRECISION_FP64 && precision != RRSPH_PRECISION_MIXED)
+        return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_create: unknown precision");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return set_error(RRSPH_ERR_NO_DEVICE, "rrsph_create: no CUDA device");
+    }
+    rrsph_solver* s = new rrsph_solver();
+    s->params = *p;
+    s->precision = precision;
+    s->dim = (int)p->dim;
+    cudaGetDevice(&s->device);
+    int rc = fill_dev_params(*p, s->P);
+    auto fail = [&](int code) {
+        rrsph_destroy(s);
+        return code;
+    };
+    if (rc) return fail(rc);
+    s->sort_bits = key_bits(p->max_cells);
+    const size_t n = p->ntotal;
+    const bool d3 = s->dim == 3;
+    const bool cont = p->density_treatment != 0;
+    const bool mixed = precision == RRSPH_PRECISION_MIXED;
+    auto& S = s->S;
+    auto& G = s->G;
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(set_error(RRSPH_ERR_CUDA, "rrsph_create: cudaStreamCreate failed"));
+#define A(ptr, count) \
+    if ((rc = dev_alloc(s, &(ptr), (count))) != 0) return fail(rc)
+    A(S.rx, n); A(S.ry, n); A(S.vx, n); A(S.vy, n); A(S.ax, n); A(S.ay, n); A(S.vpx, n); A(S.vpy, n);
+    if (d3) { A(S.rz, n); A(S.vz, n); A(S.az, n); A(S.vpz, n); }
+    if (p->average_velocity) { A(S.avx, n); A(S.avy, n); if (d3) A(S.avz, n); }
+    A(S.rho, n); A(S.p, n); A(S.drho, n); A(S.rho_pred, n); A(S.mu, n);
+    A(S.itype, n); A(S.key_of, n);
+    A(G.keys_in, n); A(G.ids_in, n); A(G.keys_a, n); A(G.ids_a, n);
+    A(G.sort_scratch, rrsph::sort_scratch_words((uint32_t)n));
+    A(G.cell_start, (size_t)s->P.max_cells); A(G.cell_end, (size_t)s->P.max_cells);
+    A(G.rx, n); A(G.ry, n); if (d3) A(G.rz, n);
+    A(G.itype, n);
+    if (!mixed) {
+        A(G.vx, n); A(G.vy, n); if (d3) A(G.vz, n);
+        A(G.rho, n); A(G.p, n);
+        if (cont) { A(G.vdx, n); A(G.vdy, n); if (d3) A(G.vdz, n); A(G.rhod, n); }
+    } else {
+        A(G.P4, n); A(G.V4, n); A(G.pf, n);
+        if (cont) A(G.VD4, n);
+    }
+    A(s->scal, 2);
+    A(s->flags, 1);
+#undef A
+    if (cudaMallocHost(&s->h_scal, sizeof(rrsph::StepScalars)) != cudaSuccess ||
+        cudaMallocHost(&s->h_flags, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMallocHost(&s->h_time, sizeof(double)) != cudaSuccess)
+        return fail(set_error(RRSPH_ERR_OUT_OF_MEMORY, "rrsph_create: pinned host allocation failed"));
+    // empty cell table, zeroed state
+    if (cudaMemsetAsync(G.cell_start, 0xFF, (size_t)s->P.max_cells * sizeof(uint32_t), s->stream) != cudaSuccess ||
+        cudaMemsetAsync(S.key_of, 0xFF, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
+        cudaMemsetAsync(s->scal, 0, 2 * sizeof(rrsph::StepScalars), s->stream) != cudaSuccess ||
+        cudaMemsetAsync(s->flags, 0, sizeof(uint32_t), s->stream) != cudaSuccess)
+        return fail(set_error(RRSPH_ERR_CUDA, "rrsph_create: memset failed"));
+    for (int i = 0; i <= kPhases; i++) {
+        if (cudaEventCreate(&s->ev[i]) != cudaSuccess) return fail(set_error(RRSPH_ERR_CUDA, "rrsph_create: event"));
+    }
+    if (cudaStreamSynchronize(s->stream) != cudaSuccess)
+        return fail(set_error(RRSPH_ERR_CUDA, "rrsph_create: synchronize failed"));
+    *out = s;
+    return RRSPH_OK;
+}
+
+extern "C" void rrsph_destroy(rrsph_solver* s) {
+    if (!s) return;
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (int i = 0; i < 2; i++)
+        if (s->graph[i]) cudaGraphExecDestroy(s->graph[i]);
+    for (int i = 0; i <= kPhases; i++)
+        if (s->ev[i]) cudaEventDestroy(s->ev[i]);
+    for (void* a : s->allocations)
+        if (a) cudaFree(a);
+    if (s->h_scal) cudaFreeHost(s->h_scal);
+    if (s->h_flags) cudaFreeHost(s->h_flags);
+    if (s->h_time) cudaFreeHost(s->h_time);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+extern "C" int rrsph_get_stream(rrsph_solver* s, void** stream) {
+    if (!s || !stream) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_get_stream: null argument");
+    *stream = (void*)s->stream;
+    return RRSPH_OK;
+}
+
+extern "C" int rrsph_upload(rrsph_solver* s, const double* r, uint32_t stride, const double* v, const double* rho,
+                            const double* pres, const int32_t* itype) {
+    int rc = check_handle(s, "rrsph_upload");
+    if (rc) return rc;
+    if (!r || !v || !rho || !itype) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_upload: null array");
+    if (stride < (uint32_t)s->dim) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_upload: stride < dim");
+    const size_t n = s->P.n;
+    if ((rc = ensure_staging(s, 2 * n * stride)) != 0) return rc;
+    auto& S = s->S;
+    cudaStream_t st = s->stream;
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(s->staging, r, n * stride * sizeof(double), cudaMemcpyHostToDevice, st));
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(s->staging + n * stride, v, n * stride * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (s->dim == 3) rrsph::launch_unpack<3>(s->P, S, s->staging, s->staging + n * stride, stride, st);
+    else rrsph::launch_unpack<2>(s->P, S, s->staging, s->staging + n * stride, stride, st);
+    s->launches++;
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(S.rho, rho, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (pres) RRSPH_CUDA_TRY(cudaMemcpyAsync(S.p, pres, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    else RRSPH_CUDA_TRY(cudaMemsetAsync(S.p, 0, n * sizeof(double), st));
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(S.itype, itype, n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    // fresh work arrays of time_integration (TimeIntegration.cpp:35-50)
+    RRSPH_CUDA_TRY(cudaMemsetAsync(S.ax, 0, n * sizeof(double), st));
+    RRSPH_CUDA_TRY(cudaMemsetAsync(S.ay, 0, n * sizeof(double), st));
+    if (S.az) RRSPH_CUDA_TRY(cudaMemsetAsync(S.az, 0, n * sizeof(double), st));
+    if (S.avx) {
+        RRSPH_CUDA_TRY(cudaMemsetAsync(S.avx, 0, n * sizeof(double), st));
+        RRSPH_CUDA_TRY(cudaMemsetAsync(S.avy, 0, n * sizeof(double), st));
+        if (S.avz) RRSPH_CUDA_TRY(cudaMemsetAsync(S.avz, 0, n * sizeof(double), st));
+    }
+    RRSPH_CUDA_TRY(cudaMemsetAsync(S.drho, 0, n * sizeof(double), st));
+    rrsph::StepScalars init{};
+    init.dt = s->params.dt;
+    std::memcpy(s->h_scal, &init, sizeof(init));
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(s->scal, s->h_scal, sizeof(init), cudaMemcpyHostToDevice, st));
+    RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
+    s->step_index = 0;
+    return RRSPH_OK;
+}
+
+extern "C" int rrsph_download(rrsph_solver* s, double* r, uint32_t stride, double* v, double* rho, double* pres,
+                              int32_t* itype) {
+    int rc = check_handle(s, "rrsph_download");
+    if (rc) return rc;
+    if ((r || v) && stride < (uint32_t)s->dim) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_download: stride < dim");
+    const size_t n = s->P.n;
+    cudaStream_t st = s->stream;
+    if (r || v) {
+        if ((rc = ensure_staging(s, 2 * n * stride)) != 0) return rc;
+        if (s->dim == 3) rrsph::launch_pack<3>(s->P, s->S, r ? s->staging : nullptr, v ? s->staging + n * stride : nullptr, stride, st);
+        else rrsph::launch_pack<2>(s->P, s->S, r ? s->staging : nullptr, v ? s->staging + n * stride : nullptr, stride, st);
+        s->launches++;
+        if (r) RRSPH_CUDA_TRY(cudaMemcpyAsync(r, s->staging, n * stride * sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (v) RRSPH_CUDA_TRY(cudaMemcpyAsync(v, s->staging + n * stride, n * stride * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
+    if (rho) RRSPH_CUDA_TRY(cudaMemcpyAsync(rho, s->S.rho, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (pres) RRSPH_CUDA_TRY(cudaMemcpyAsync(pres, s->S.p, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (itype) RRSPH_CUDA_TRY(cudaMemcpyAsync(itype, s->S.itype, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
+    return RRSPH_OK;
+}
+
+extern "C" int rrsph_step(rrsph_solver* s, uint64_t nsteps, double* time_io) {
+    int rc = check_handle(s, "rrsph_step");
+    if (rc) return rc;
+    if (!time_io) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_step: null time");
+    cudaStream_t st = s->stream;
+    const int par0 = (int)(s->step_index & 1);
+    *s->h_time = *time_io;
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(&s->scal[par0].time, s->h_time, sizeof(double), cudaMemcpyHostToDevice, st));
+    RRSPH_CUDA_TRY(cudaMemsetAsync(s->flags, 0, sizeof(uint32_t), st));
+    for (uint64_t k = 0; k < nsteps; k++) {
+        const int par = (int)(s->step_index & 1);
+        if (s->timing) {
+            enqueue_step_dim(s, par, s->ev);
+            RRSPH_CUDA_TRY(cudaEventSynchronize(s->ev[kPhases]));
+            for (int i = 0; i < kPhases; i++) {
+                float ms = 0;
+                cudaEventElapsedTime(&ms, s->ev[i], s->ev[i + 1]);
+                s->phase_ms[i] += ms;
+            }
+            s->timed_steps++;
+        } else if (s->graphs) {
+            if (!s->graph[par]) {
+                cudaGraph_t g = nullptr;
+                const unsigned long long before = s->launches;
+                RRSPH_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                enqueue_step_dim(s, par, nullptr);
+                RRSPH_CUDA_TRY(cudaStreamEndCapture(st, &g));
+                const cudaError_t e = cudaGraphInstantiate(&s->graph[par], g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) return set_error(RRSPH_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+                s->launches_in_graph[par] = s->launches - before;
+                s->launches = before;
+            }
+            RRSPH_CUDA_TRY(cudaGraphLaunch(s->graph[par], st));
+            s->launches += s->launches_in_graph[par];
+        } else {
+            enqueue_step_dim(s, par, nullptr);
+        }
+        s->step_index++;
+    }
+    const int parn = (int)(s->step_index & 1);
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(s->h_scal, &s->scal[parn], sizeof(rrsph::StepScalars), cudaMemcpyDeviceToHost, st));
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(s->h_flags, s->flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
+    RRSPH_CUDA_TRY(cudaGetLastError());
+    *time_io = s->h_scal->time;
+    return flags_to_status(s, *s->h_flags);
+}
+
+extern "C" int rrsph_status(rrsph_solver* s, uint32_t* flags, int clear) {
+    int rc = check_handle(s, "rrsph_status");
+    if (rc) return rc;
+    if (!flags) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_status: null flags");
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(s->h_flags, s->flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
+    if (clear) RRSPH_CUDA_TRY(cudaMemsetAsync(s->flags, 0, sizeof(uint32_t), s->stream));
+    RRSPH_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    *flags = *s->h_flags;
+    return RRSPH_OK;
+}
+
+extern "C" int rrsph_get_dt(rrsph_solver* s, double* dt) {
+    int rc = check_handle(s, "rrsph_get_dt");
+    if (rc) return rc;
+    if (!dt) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_get_dt: null dt");
+    const int par = (int)(s->step_index & 1);
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(s->h_scal, &s->scal[par], sizeof(rrsph::StepScalars), cudaMemcpyDeviceToHost, s->stream));
+    RRSPH_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    *dt = s->h_scal->dt;
+    return RRSPH_OK;
+}
+
+// ---------------------------------------------------------- loop pieces ----
+
+namespace {
+
+template <int DIM>
+void enqueue_component_grid(rrsph_solver* s, bool with_p) {
+    rrsph::GatherSrc fsrc{s->S.vx, s->S.vy, s->S.vz, s->S.rho, with_p ? s->S.p : nullptr};
+    enqueue_grid<DIM>(s, 0, s->scal, fsrc);
+}
+void enqueue_component_grid_dim(rrsph_solver* s, bool with_p) {
+    if (s->dim == 3) enqueue_component_grid<3>(s, with_p);
+    else enqueue_component_grid<2>(s, with_p);
+}
+
+int finish_component(rrsph_solver* s, const char* fn) {
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(s->h_flags, s->flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
+    RRSPH_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(RRSPH_ERR_CUDA, std::string(fn) + ": " + cudaGetErrorString(e));
+    const uint32_t f = *s->h_flags;
+    if (f & RRSPH_FLAG_OUT_OF_DOMAIN) return set_error(RRSPH_ERR_OUT_OF_DOMAIN, "cell_idx was >= params.max_cells");
+    if (f & RRSPH_FLAG_NEIGHBOUR_OVERFLOW) return set_error(RRSPH_ERR_NEIGHBOUR_OVERFLOW, "making neighbours grid: error occured");
+    return RRSPH_OK;
+}
+
+}  // namespace
+
+extern "C" int rrsph_grid_find(rrsph_solver* s, uint32_t* keys, uint32_t* grid, uint32_t* cells_start) {
+    int rc = check_handle(s, "rrsph_grid_find");
+    if (rc) return rc;
+    cudaStream_t st = s->stream;
+    RRSPH_CUDA_TRY(cudaMemsetAsync(s->flags, 0, sizeof(uint32_t), st));
+    enqueue_component_grid_dim(s, false);
+    const size_t n = s->P.n;
+    uint32_t* d_cs = nullptr;
+    if (cells_start) {
+        RRSPH_CUDA_TRY(cudaMallocAsync(&d_cs, ((size_t)s->P.max_cells + 1) * sizeof(uint32_t), st));
+        rrsph::launch_cells_start(s->P, s->G, d_cs, st);
+        s->launches++;
+        RRSPH_CUDA_TRY(cudaMemcpyAsync(cells_start, d_cs, ((size_t)s->P.max_cells + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        RRSPH_CUDA_TRY(cudaFreeAsync(d_cs, st));
+    }
+    if (keys) RRSPH_CUDA_TRY(cudaMemcpyAsync(keys, s->S.key_of, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    if (grid) RRSPH_CUDA_TRY(cudaMemcpyAsync(grid, s->G.id, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    return finish_component(s, "rrsph_grid_find");
+}
+
+extern "C" int rrsph_neighbours(rrsph_solver* s, uint32_t* counts, uint32_t* list, uint32_t max_per,
+                                uint64_t* total_pairs) {
+    int rc = check_handle(s, "rrsph_neighbours");
+    if (rc) return rc;
+    if (!counts || !list || max_per == 0) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_neighbours: bad arguments");
+    cudaStream_t st = s->stream;
+    const size_t n = s->P.n;
+    RRSPH_CUDA_TRY(cudaMemsetAsync(s->flags, 0, sizeof(uint32_t), st));
+    enqueue_component_grid_dim(s, false);
+    uint32_t *d_counts = nullptr, *d_list = nullptr;
+    RRSPH_CUDA_TRY(cudaMallocAsync(&d_counts, n * sizeof(uint32_t), st));
+    RRSPH_CUDA_TRY(cudaMallocAsync(&d_list, n * (size_t)max_per * sizeof(uint32_t), st));
+    if (s->dim == 3) rrsph::launch_neighbour_list<3>(s->P, s->G, d_counts, d_list, max_per, s->flags, st);
+    else rrsph::launch_neighbour_list<2>(s->P, s->G, d_counts, d_list, max_per, s->flags, st);
+    s->launches++;
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(counts, d_counts, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(list, d_list, n * (size_t)max_per * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    RRSPH_CUDA_TRY(cudaFreeAsync(d_counts, st));
+    RRSPH_CUDA_TRY(cudaFreeAsync(d_list, st));
+    rc = finish_component(s, "rrsph_neighbours");
+    if (total_pairs) {
+        uint64_t t = 0;
+        for (size_t j = 0; j < n; j++) t += counts[j];
+        *total_pairs = t;
+    }
+    return rc;
+}
+
+extern "C" int rrsph_density(rrsph_solver* s, double* out_rho_or_drho, double* out_p) {
+    int rc = check_handle(s, "rrsph_density");
+    if (rc) return rc;
+    cudaStream_t st = s->stream;
+    const size_t n = s->P.n;
+    RRSPH_CUDA_TRY(cudaMemsetAsync(s->flags, 0, sizeof(uint32_t), st));
+    enqueue_component_grid_dim(s, false);
+    if (s->dim == 3) enqueue_density<3>(s, s->scal);
+    else enqueue_density<2>(s, s->scal);
+    const bool cont = s->P.density_treatment != 0;
+    if (out_rho_or_drho)
+        RRSPH_CUDA_TRY(cudaMemcpyAsync(out_rho_or_drho, cont ? s->S.drho : s->S.rho, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (out_p) RRSPH_CUDA_TRY(cudaMemcpyAsync(out_p, s->S.p, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    return finish_component(s, "rrsph_density");
+}
+
+extern "C" int rrsph_forces(rrsph_solver* s, uint32_t terms, double* a, uint32_t stride, double* av, double* mu) {
+    int rc = check_handle(s, "rrsph_forces");
+    if (rc) return rc;
+    if (!a || stride < (uint32_t)s->dim) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_forces: bad a/stride");
+    if (av && !s->S.avx) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_forces: average_velocity is off");
+    cudaStream_t st = s->stream;
+    const size_t n = s->P.n;
+    RRSPH_CUDA_TRY(cudaMemsetAsync(s->flags, 0, sizeof(uint32_t), st));
+    enqueue_component_grid_dim(s, true);
+    if (s->dim == 3) enqueue_forces<3>(s, terms, s->scal, 1);
+    else enqueue_forces<2>(s, terms, s->scal, 1);
+    if ((rc = ensure_staging(s, 2 * n * stride)) != 0) return rc;
+    // pack a (and av) through the staging buffer with the pack kernel's layout
+    rrsph::State tmp = s->S;
+    tmp.rx = s->S.ax; tmp.ry = s->S.ay; tmp.rz = s->S.az;
+    tmp.vx = s->S.avx; tmp.vy = s->S.avy; tmp.vz = s->S.avz;
+    double* dv = av ? s->staging + n * stride : nullptr;
+    if (s->dim == 3) rrsph::launch_pack<3>(s->P, tmp, s->staging, dv, stride, st);
+    else rrsph::launch_pack<2>(s->P, tmp, s->staging, dv, stride, st);
+    s->launches++;
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(a, s->staging, n * stride * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (av) RRSPH_CUDA_TRY(cudaMemcpyAsync(av, dv, n * stride * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (mu) RRSPH_CUDA_TRY(cudaMemcpyAsync(mu, s->S.mu, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    return finish_component(s, "rrsph_forces");
+}
+
+// ------------------------------------------------------------- timing ------
+
+extern "C" int rrsph_phase_count(rrsph_solver* s, int* count) {
+    if (!s || !count) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_phase_count: null argument");
+    *count = kPhases;
+    return RRSPH_OK;
+}
+extern "C" const char* rrsph_phase_name(rrsph_solver* s, int phase) {
+    (void)s;
+    return (phase >= 0 && phase < kPhases) ? kPhaseNames[phase] : "";
+}
+extern "C" int rrsph_set_phase_timing(rrsph_solver* s, int enable) {
+    if (!s) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_set_phase_timing: null solver");
+    s->timing = enable != 0;
+    return RRSPH_OK;
+}
+extern "C" int rrsph_phase_times(rrsph_solver* s, double* ms_per_phase, int count, uint64_t* steps, int reset) {
+    if (!s || !ms_per_phase) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_phase_times: null argument");
+    for (int i = 0; i < count && i < kPhases; i++) ms_per_phase[i] = s->phase_ms[i];
+    if (steps) *steps = s->timed_steps;
+    if (reset) {
+        for (double& v : s->phase_ms) v = 0;
+        s->timed_steps = 0;
+    }
+    return RRSPH_OK;
+}
+extern "C" int rrsph_kernel_launches(rrsph_solver* s, uint64_t* launches) {
+    if (!s || !launches) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_kernel_launches: null argument");
+    *launches = s->launches;
+    return RRSPH_OK;
+}

@@ -1,0 +1,159 @@
+// sort.cu — stable LSD radix sort of (cell key, particle id) pairs.
+//
+// Replaces the reference's serial counting sort over max_cells
+// (sources/RRSPH_OMP/src/GridFind.cpp:47-88) and the OpenCL bitonic sort
+// (sources/RRSPH_CL/cl/GridFind.cl:73-93, power-of-two sizes only): any n,
+// stable, so that ids stay ascending within a cell exactly as after the
+// reference's reverse scatter.
+//
+// One 8-bit digit per pass, three kernels per pass, no inter-block waiting:
+//   1. k_tile_hist:   digit counts of each 2048-key tile        -> counts[d][tile]
+//   2. k_digit_scan:  one warp per digit scans its row over tiles (exclusive)
+//                     and records the digit total
+//   3. k_scatter:     each tile ranks its keys stably (warp match + per-warp
+//                     counts, in (round, warp, lane) = input order) and writes
+//                     them to total-prefix[d] + tile-prefix[d][tile] + rank.
+#include "sort.cuh"
+
+namespace rrsph {
+
+namespace {
+
+constexpr int kWarps = kSortThreads / 32;
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_tile_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift,
+                                                            uint32_t tiles, uint32_t* __restrict__ counts) {
+    __shared__ uint32_t h[kRadix];
+    for (int d = threadIdx.x; d < kRadix; d += kSortThreads) h[d] = 0;
+    __syncthreads();
+    const uint32_t base = blockIdx.x * (uint32_t)kSortTile;
+    const uint32_t lane = threadIdx.x & 31;
+#pragma unroll
+    for (int r = 0; r < kSortItems; r++) {
+        const uint32_t idx = base + r * kSortThreads + threadIdx.x;
+        const bool valid = idx < n;
+        const uint32_t d = valid ? ((keys[idx] >> shift) & (kRadix - 1)) : kRadix;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        // one shared-memory add per distinct digit in the warp
+        if (valid && (__ffs(peers) - 1) == (int)lane) atomicAdd(&h[d], __popc(peers));
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < kRadix; d += kSortThreads) counts[(size_t)d * tiles + blockIdx.x] = h[d];
+}
+
+// counts[d][t] -> exclusive prefix over t; totals[d] = row sum.
+__global__ void k_digit_scan(uint32_t* __restrict__ counts, uint32_t tiles, uint32_t* __restrict__ totals) {
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31;
+    if (warp >= kRadix) return;
+    uint32_t* row = counts + (size_t)warp * tiles;
+    uint32_t carry = 0;
+    for (uint32_t t0 = 0; t0 < tiles; t0 += 32) {
+        const uint32_t t = t0 + lane;
+        const uint32_t v = t < tiles ? row[t] : 0;
+        uint32_t incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if ((int)lane >= o) incl += x;
+        }
+        if (t < tiles) row[t] = carry + incl - v;
+        carry += __shfl_sync(0xFFFFFFFFu, incl, 31);
+    }
+    if (lane == 0) totals[warp] = carry;
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_scatter(const uint32_t* __restrict__ keys_in,
+                                                          const uint32_t* __restrict__ vals_in,
+                                                          uint32_t* __restrict__ keys_out,
+                                                          uint32_t* __restrict__ vals_out, uint32_t n, int shift,
+                                                          uint32_t tiles, const uint32_t* __restrict__ prefix,
+                                                          const uint32_t* __restrict__ totals) {
+    __shared__ uint32_t base_of[kRadix];   // output start of each digit for this tile
+    __shared__ uint32_t running[kRadix];   // keys of each digit already placed by earlier rounds
+    __shared__ uint32_t wcount[kWarps][kRadix];
+    __shared__ uint32_t scan_tmp[kRadix];
+
+    const int tid = threadIdx.x;
+    const uint32_t warp = tid >> 5, lane = tid & 31;
+    // exclusive scan of the 256 digit totals (kSortThreads == kRadix)
+    {
+        const uint32_t v = totals[tid];
+        uint32_t incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if ((int)lane >= o) incl += x;
+        }
+        if (lane == 31) scan_tmp[warp] = incl;
+        __syncthreads();
+        uint32_t warp_off = 0;
+        for (uint32_t w = 0; w < warp; w++) warp_off += scan_tmp[w];
+        base_of[tid] = warp_off + incl - v + prefix[(size_t)tid * tiles + blockIdx.x];
+        running[tid] = 0;
+    }
+    __syncthreads();
+
+    const uint32_t base = blockIdx.x * (uint32_t)kSortTile;
+    for (int r = 0; r < kSortItems; r++) {
+        const uint32_t idx = base + r * kSortThreads + tid;
+        const bool valid = idx < n;
+        uint32_t key = 0, val = 0, d = kRadix;
+        if (valid) {
+            key = keys_in[idx];
+            val = vals_in[idx];
+            d = (key >> shift) & (kRadix - 1);
+        }
+        for (int i = tid; i < kWarps * kRadix; i += kSortThreads) (&wcount[0][0])[i] = 0;
+        __syncthreads();
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        const uint32_t rank = __popc(peers & lanemask_lt());
+        if (valid && rank == 0) wcount[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            uint32_t pos = base_of[d] + running[d] + rank;
+            for (uint32_t w = 0; w < warp; w++) pos += wcount[w][d];
+            keys_out[pos] = key;
+            vals_out[pos] = val;
+        }
+        __syncthreads();
+        {
+            uint32_t s = 0;
+#pragma unroll
+            for (int w = 0; w < kWarps; w++) s += wcount[w][tid];
+            running[tid] += s;
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, uint32_t* scratch,
+                      uint32_t n, int bits, cudaStream_t stream, uint32_t** keys_out, uint32_t** vals_out,
+                      unsigned long long* launches) {
+    const uint32_t tiles = sort_tiles(n);
+    uint32_t* counts = scratch;
+    uint32_t* totals = scratch + (size_t)kRadix * tiles;
+    uint32_t *ki = keys, *vi = vals, *ko = keys_alt, *vo = vals_alt;
+    if (n > 0) {
+        for (int shift = 0; shift < bits; shift += 8) {
+            k_tile_hist<<<tiles, kSortThreads, 0, stream>>>(ki, n, shift, tiles, counts);
+            k_digit_scan<<<kRadix * 32 / 256, 256, 0, stream>>>(counts, tiles, totals);
+            k_scatter<<<tiles, kSortThreads, 0, stream>>>(ki, vi, ko, vo, n, shift, tiles, counts, totals);
+            if (launches) *launches += 3;
+            uint32_t* t = ki; ki = ko; ko = t;
+            t = vi; vi = vo; vo = t;
+        }
+    }
+    *keys_out = ki;
+    *vals_out = vi;
+}
+
+}  // namespace rrsph

@@ -1,0 +1,27 @@
+// sort.cuh — stable LSD radix sort of (32-bit cell key, 32-bit particle id) pairs.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rrsph {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;  // keys per tile
+constexpr int kRadix = 256;                           // 8-bit digits
+
+inline uint32_t sort_tiles(uint32_t n) { return (n + kSortTile - 1) / kSortTile; }
+// Scratch words the sort needs for n keys: per-tile digit counts + digit totals.
+inline size_t sort_scratch_words(uint32_t n) { return (size_t)kRadix * sort_tiles(n) + kRadix; }
+
+// Sorts n pairs by the low `bits` bits of the keys, stably (equal keys keep
+// their input order). keys/vals hold the input; keys_alt/vals_alt are equal
+// sized buffers. On return *keys_out/*vals_out point at whichever pair of
+// buffers holds the result. scratch holds sort_scratch_words(n) words.
+// Launches 3 kernels per 8-bit digit on `stream`; adds them to *launches.
+void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt,
+                      uint32_t* scratch, uint32_t n, int bits, cudaStream_t stream,
+                      uint32_t** keys_out, uint32_t** vals_out, unsigned long long* launches);
+
+}  // namespace rrsph

@@ -1,0 +1,162 @@
+// layers.cpp — particle layer CSV files of an experiment directory.
+//
+// Format of the reference's dump/data layers (sources/RRSPH_COMMON/src/Output.cpp:80-221):
+// header x,y[,z],itype[,vx,vy[,vz]][,rho][,p]; fields separated by ',', rows
+// ended by '\n'; doubles printed by std::to_string ("%f"), itype as an integer.
+// Reading follows loadArrays (sources/RRSPH_COMMON/src/Input.cpp:203-236):
+// columns are looked up by name and the row count must equal ntotal.
+#include "../../include/rrsph_cuda.h"
+#include "error.hpp"
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <filesystem>
+#include <string>
+#include <vector>
+
+using rrsph::set_error;
+
+namespace {
+
+// std::to_string(double) is specified as printf("%f")
+void put_f(std::string& out, double v) {
+    char buf[512];
+    const int n = std::snprintf(buf, sizeof(buf), "%f", v);
+    out.append(buf, (size_t)(n > 0 ? n : 0));
+}
+
+}  // namespace
+
+extern "C" int rrsph_layer_time_from_path(const char* path, double* t) {
+    if (!path || !t) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_layer_time_from_path: null argument");
+    const std::string stem = std::filesystem::path(path).stem().string();
+    char* end = nullptr;
+    const double v = std::strtod(stem.c_str(), &end);
+    if (end == stem.c_str()) return set_error(RRSPH_ERR_PARSE, "layer name is not a time: " + stem);
+    *t = v;
+    return RRSPH_OK;
+}
+
+extern "C" int rrsph_layer_read(const char* csv_path, const rrsph_params* p, double* r, uint32_t stride, double* v,
+                                double* rho, double* pres, int32_t* itype) {
+    if (!csv_path || !p || !r || !v || !rho || !itype)
+        return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_layer_read: null argument");
+    if (stride < p->dim) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_layer_read: stride < dim");
+    FILE* f = std::fopen(csv_path, "rb");
+    if (!f) return set_error(RRSPH_ERR_IO, std::string("cannot open layer ") + csv_path);
+    std::string data;
+    {
+        char buf[1 << 16];
+        size_t got;
+        while ((got = std::fread(buf, 1, sizeof(buf), f)) > 0) data.append(buf, got);
+        std::fclose(f);
+    }
+    // header
+    size_t pos = data.find('\n');
+    if (pos == std::string::npos) return set_error(RRSPH_ERR_PARSE, "layer has no header line");
+    std::vector<std::string> cols;
+    {
+        std::string h = data.substr(0, pos);
+        if (!h.empty() && h.back() == '\r') h.pop_back();
+        size_t s = 0;
+        for (;;) {
+            const size_t e = h.find(',', s);
+            std::string name = h.substr(s, e == std::string::npos ? std::string::npos : e - s);
+            if (name.size() >= 2 && name.front() == '"' && name.back() == '"') name = name.substr(1, name.size() - 2);
+            cols.push_back(name);
+            if (e == std::string::npos) break;
+            s = e + 1;
+        }
+    }
+    const bool d3 = p->dim == 3;
+    auto col = [&](const char* n) -> int {
+        for (size_t i = 0; i < cols.size(); i++)
+            if (cols[i] == n) return (int)i;
+        return -1;
+    };
+    const int cx = col("x"), cy = col("y"), cz = d3 ? col("z") : -1, ct = col("itype"), cvx = col("vx"),
+              cvy = col("vy"), cvz = d3 ? col("vz") : -1, cr = col("rho"), cp = col("p");
+    if (cx < 0 || cy < 0 || ct < 0 || cvx < 0 || cvy < 0 || cr < 0 || (d3 && (cz < 0 || cvz < 0)))
+        return set_error(RRSPH_ERR_PARSE, std::string("layer ") + csv_path + " lacks a column of x,y,[z],itype,vx,vy,[vz],rho");
+    std::vector<const char*> field(cols.size());
+    uint64_t row = 0;
+    size_t i = pos + 1;
+    const size_t n = data.size();
+    while (i < n) {
+        // split one line in place
+        size_t k = 0;
+        size_t s = i;
+        while (i < n && data[i] != '\n') {
+            if (data[i] == ',') {
+                if (k < field.size()) field[k++] = data.c_str() + s;
+                s = i + 1;
+            }
+            i++;
+        }
+        const bool empty_line = (i == s) && k == 0;
+        if (k < field.size()) field[k++] = data.c_str() + s;
+        i++;  // skip '\n'
+        if (empty_line) continue;
+        if (k != field.size()) return set_error(RRSPH_ERR_PARSE, "layer row " + std::to_string(row) + " has a wrong number of fields");
+        if (row >= p->ntotal) return set_error(RRSPH_ERR_PARSE, "dump corrupted: dump ntotal doesn't match params.ntotal!");
+        double* rr = r + row * stride;
+        double* vv = v + row * stride;
+        rr[0] = std::strtod(field[cx], nullptr);
+        rr[1] = std::strtod(field[cy], nullptr);
+        if (d3) rr[2] = std::strtod(field[cz], nullptr);
+        itype[row] = (int32_t)std::strtol(field[ct], nullptr, 10);
+        vv[0] = std::strtod(field[cvx], nullptr);
+        vv[1] = std::strtod(field[cvy], nullptr);
+        if (d3) vv[2] = std::strtod(field[cvz], nullptr);
+        rho[row] = std::strtod(field[cr], nullptr);
+        if (pres) pres[row] = cp >= 0 ? std::strtod(field[cp], nullptr) : 0.0;
+        row++;
+    }
+    if (row != p->ntotal) return set_error(RRSPH_ERR_PARSE, "dump corrupted: dump ntotal doesn't match params.ntotal!");
+    return RRSPH_OK;
+}
+
+extern "C" int rrsph_layer_write(const char* csv_path, const rrsph_params* p, const double* r, uint32_t stride,
+                                 const double* v, const double* rho, const double* pres, const int32_t* itype,
+                                 int dump) {
+    if (!csv_path || !p || !r || !itype) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_layer_write: null argument");
+    if (stride < p->dim) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_layer_write: stride < dim");
+    const bool d3 = p->dim == 3;
+    const bool wv = dump ? true : (p->save_velocity && v);
+    const bool wr = dump ? true : (p->save_density && rho);
+    const bool wp = dump ? true : (p->save_pressure && pres);
+    if ((wv && !v) || (wr && !rho) || (wp && !pres))
+        return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_layer_write: a dump needs r, itype, v, rho and p");
+    std::string out;
+    out.reserve((size_t)p->ntotal * 96 + 64);
+    out += d3 ? "x,y,z,itype" : "x,y,itype";
+    if (wv) out += d3 ? ",vx,vy,vz" : ",vx,vy";
+    if (wr) out += ",rho";
+    if (wp) out += ",p";
+    out += '\n';
+    char ibuf[32];
+    for (uint64_t i = 0; i < p->ntotal; i++) {
+        const double* ri = r + i * stride;
+        put_f(out, ri[0]); out += ',';
+        put_f(out, ri[1]); out += ',';
+        if (d3) { put_f(out, ri[2]); out += ','; }
+        const int n = std::snprintf(ibuf, sizeof(ibuf), "%ld", (long)itype[i]);
+        out.append(ibuf, (size_t)n);
+        if (wv) {
+            const double* vi = v + i * stride;
+            out += ','; put_f(out, vi[0]);
+            out += ','; put_f(out, vi[1]);
+            if (d3) { out += ','; put_f(out, vi[2]); }
+        }
+        if (wr) { out += ','; put_f(out, rho[i]); }
+        if (wp) { out += ','; put_f(out, pres[i]); }
+        out += '\n';
+    }
+    FILE* f = std::fopen(csv_path, "wb");
+    if (!f) return set_error(RRSPH_ERR_IO, std::string("cannot write layer ") + csv_path);
+    const size_t put = std::fwrite(out.data(), 1, out.size(), f);
+    std::fclose(f);
+    if (put != out.size()) return set_error(RRSPH_ERR_IO, std::string("short write of layer ") + csv_path);
+    return RRSPH_OK;
+}

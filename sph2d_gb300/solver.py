@@ -1,0 +1,209 @@
+"""Python handle over the C ABI of the GPU step (``include/rrsph_cuda.h``).
+
+Arrays are numpy float64 / int32 / uint32; positions and velocities are
+``(ntotal, dim)`` particle-major (stride = dim) unless a stride is given.
+Every call goes through librrsph_cuda.so; there is no other implementation.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import json
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+from . import capi
+from .capi import RrsphParams, check, lib
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _u32p(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_uint32))
+
+
+def _i32p(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def default_params() -> RrsphParams:
+    p = RrsphParams()
+    check(lib().rrsph_params_defaults(C.byref(p)))
+    return p
+
+
+def load_params(experiment_dir: str | Path) -> RrsphParams:
+    """ParticleParams.json + ModelParams.json of an experiment directory."""
+    p = default_params()
+    check(lib().rrsph_experiment_load_params(str(experiment_dir).encode(), C.byref(p)))
+    return p
+
+
+def params_from_json(model: dict, particle: dict) -> RrsphParams:
+    """Parses the two JSON objects through the library's own loader."""
+    with tempfile.TemporaryDirectory() as d:
+        Path(d, "ModelParams.json").write_text(json.dumps(model, indent=2))
+        Path(d, "ParticleParams.json").write_text(json.dumps(particle, indent=2))
+        return load_params(d)
+
+
+def derive(p: RrsphParams, r: np.ndarray | None) -> RrsphParams:
+    """fillInComputingParams/postFillInModelParams on a copy of p."""
+    q = p.copy()
+    if r is not None:
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        stride = r.shape[1]
+    else:
+        stride = q.dim
+    check(lib().rrsph_params_derive(C.byref(q), _dp(r), stride))
+    return q
+
+
+def read_layer(path: str | Path, p: RrsphParams):
+    n, dim = p.ntotal, p.dim
+    r = np.zeros((n, dim))
+    v = np.zeros((n, dim))
+    rho = np.zeros(n)
+    pres = np.zeros(n)
+    itype = np.zeros(n, dtype=np.int32)
+    check(lib().rrsph_layer_read(str(path).encode(), C.byref(p), _dp(r), dim, _dp(v), _dp(rho), _dp(pres), _i32p(itype)))
+    return r, v, rho, pres, itype
+
+
+def write_layer(path: str | Path, p: RrsphParams, r, v, rho, pres, itype, dump: bool = True) -> None:
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    v = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
+    rho = None if rho is None else np.ascontiguousarray(rho, dtype=np.float64)
+    pres = None if pres is None else np.ascontiguousarray(pres, dtype=np.float64)
+    itype = np.ascontiguousarray(itype, dtype=np.int32)
+    check(lib().rrsph_layer_write(str(path).encode(), C.byref(p), _dp(r), r.shape[1], _dp(v), _dp(rho), _dp(pres),
+                                  _i32p(itype), 1 if dump else 0))
+
+
+class Solver:
+    """One GPU solver handle (rrsph_create ... rrsph_destroy)."""
+
+    def __init__(self, params: RrsphParams, precision: str = "fp64"):
+        self.params = params.copy()
+        self.precision = capi.PRECISION_MIXED if precision == "mixed" else capi.PRECISION_FP64
+        h = C.c_void_p()
+        check(lib().rrsph_create(C.byref(self.params), self.precision, C.byref(h)))
+        self._h = h
+        self.n = int(params.ntotal)
+        self.dim = int(params.dim)
+
+    # -- lifetime
+    def close(self) -> None:
+        if self._h:
+            lib().rrsph_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        s = C.c_void_p()
+        check(lib().rrsph_get_stream(self._h, C.byref(s)))
+        return int(s.value or 0)
+
+    # -- state
+    def upload(self, r, v, rho, itype, pres=None) -> None:
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        itype = np.ascontiguousarray(itype, dtype=np.int32)
+        pres = None if pres is None else np.ascontiguousarray(pres, dtype=np.float64)
+        assert r.shape == (self.n, r.shape[1]) and r.shape[1] >= self.dim and v.shape == r.shape
+        check(lib().rrsph_upload(self._h, _dp(r), r.shape[1], _dp(v), _dp(rho), _dp(pres), _i32p(itype)))
+
+    def download(self) -> dict:
+        r = np.zeros((self.n, self.dim))
+        v = np.zeros((self.n, self.dim))
+        rho = np.zeros(self.n)
+        pres = np.zeros(self.n)
+        itype = np.zeros(self.n, dtype=np.int32)
+        check(lib().rrsph_download(self._h, _dp(r), self.dim, _dp(v), _dp(rho), _dp(pres), _i32p(itype)))
+        return {"r": r, "v": v, "rho": rho, "p": pres, "itype": itype}
+
+    def step(self, nsteps: int, time: float = 0.0) -> float:
+        t = C.c_double(time)
+        check(lib().rrsph_step(self._h, nsteps, C.byref(t)))
+        return t.value
+
+    def status(self, clear: bool = False) -> int:
+        f = C.c_uint32()
+        check(lib().rrsph_status(self._h, C.byref(f), 1 if clear else 0))
+        return f.value
+
+    def dt(self) -> float:
+        d = C.c_double()
+        check(lib().rrsph_get_dt(self._h, C.byref(d)))
+        return d.value
+
+    # -- loop pieces
+    def grid_find(self, with_cells_start: bool = True):
+        keys = np.zeros(self.n, dtype=np.uint32)
+        grid = np.zeros(self.n, dtype=np.uint32)
+        cs = np.zeros(int(self.params.max_cells) + 1, dtype=np.uint32) if with_cells_start else None
+        check(lib().rrsph_grid_find(self._h, _u32p(keys), _u32p(grid), _u32p(cs)))
+        return keys, grid, cs
+
+    def neighbours(self, max_per: int | None = None):
+        max_per = int(max_per or self.params.max_neighbours)
+        counts = np.zeros(self.n, dtype=np.uint32)
+        lst = np.zeros(self.n * max_per, dtype=np.uint32)
+        tot = C.c_uint64()
+        check(lib().rrsph_neighbours(self._h, _u32p(counts), _u32p(lst), max_per, C.byref(tot)))
+        return counts, lst.reshape(self.n, max_per), int(tot.value)
+
+    def density(self):
+        out = np.zeros(self.n)
+        pres = np.zeros(self.n)
+        check(lib().rrsph_density(self._h, _dp(out), _dp(pres)))
+        return out, pres
+
+    def forces(self, terms: int = capi.TERM_ALL, with_av: bool = False):
+        a = np.zeros((self.n, self.dim))
+        av = np.zeros((self.n, self.dim)) if with_av else None
+        mu = np.zeros(self.n)
+        check(lib().rrsph_forces(self._h, terms, _dp(a), self.dim, _dp(av), _dp(mu)))
+        return a, av, mu
+
+    # -- timing
+    def phase_names(self) -> list[str]:
+        c = C.c_int()
+        check(lib().rrsph_phase_count(self._h, C.byref(c)))
+        return [lib().rrsph_phase_name(self._h, i).decode() for i in range(c.value)]
+
+    def set_phase_timing(self, enable: bool) -> None:
+        check(lib().rrsph_set_phase_timing(self._h, 1 if enable else 0))
+
+    def phase_times(self, reset: bool = True):
+        names = self.phase_names()
+        ms = (C.c_double * len(names))()
+        steps = C.c_uint64()
+        check(lib().rrsph_phase_times(self._h, ms, len(names), C.byref(steps), 1 if reset else 0))
+        return dict(zip(names, list(ms))), int(steps.value)
+
+    def kernel_launches(self) -> int:
+        c = C.c_uint64()
+        check(lib().rrsph_kernel_launches(self._h, C.byref(c)))
+        return int(c.value)
