@@ -1,0 +1,436 @@
+"""Benchmark of the WCSPH step on one node.
+
+Workload: the 2D piston wave flume — 4000 x 100 fluid lattice at dx = 0.005 m
+(400,000 fluid particles, 20 m x 0.5 m of water) in a 1.2 m high tank with
+Lennard-Jones floor, right wall and piston column at dx/2 (8,970 particles),
+h = 1.4 dx, summation density, cubic spline, Tait EOS, Monaghan viscosity
+(alpha 0.3), piston displacement 0.05 sin(2 pi t / 1.5 s), dt = 0.2 h / c0.
+Inputs are seeded synthetic particles with those shapes (sph2d_gb300.cases).
+
+One step is one pass of the loop body (predict, grid, density, forces,
+piston, whole step). The headline is the FP32-mixed step; the plain FP64 GPU
+step is timed beside it, and the mixed step's per-field error against the FP64
+GPU step is reported.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Multi-GPU: the step does not shard (one tank), so N ranks run N independent
+replicas (weak scaling); value sums the ranks' pairs over the slowest rank's
+time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "pair-interactions/s and ms/step: FP32-mixed vs FP64 GPU step at stated error"
+UNIT = "pair-interactions/s"
+L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
+
+# Algorithmic bytes per particle of the dominant kernel (the force gather) of
+# the FP32-mixed 2D step: reads cell key 4, id 4, position+type float4 16,
+# velocity+density float4 16, pressure 4; writes a.x, a.y as double 16.
+FORCES_MIXED_BYTES_PER_PARTICLE = 60
+FORCES_FP64_BYTES_PER_PARTICLE_2D = 4 + 4 + 16 + 4 + 16 + 8 + 8 + 16
+
+
+def workload_config(case, p, pairs):
+    return {
+        "workload": "2D piston wave flume: 20 m x 0.5 m water (4000 x 100 at dx=0.005 m), 1.2 m tank, "
+                    "LJ walls + piston at dx/2, summation density, piston 0.05*sin(2*pi*t/1.5 s)",
+        "n_particles": int(case.ntotal),
+        "n_fluid": int(case.notes["nfluid"]),
+        "pairs_per_step": int(pairs),
+        "h": case.notes["h"],
+        "dt": case.notes["dt"],
+        "precision": "mixed (f32 pairs, f64 state/integration)",
+        "l2": "flushed (256 MiB device write) before every timed step",
+        "parallelism": "replicas",
+    }
+
+
+# --------------------------------------------------------------- clocks ----
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), f))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for _, _, f in rows for n, v in zip(names, f[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ----------------------------------------------------------- GPU arm -------
+
+def _time_steps(solver, flush, steps: int) -> float:
+    """Device milliseconds of `steps` single-step graph launches, each after an
+    L2 flush, timed with CUDA events on the solver's stream."""
+    import torch
+
+    ext = torch.cuda.ExternalStream(solver.stream)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    with torch.cuda.stream(ext):
+        for k in range(steps):
+            flush.add_(1)
+            starts[k].record(ext)
+            solver.step_async(1)
+            ends[k].record(ext)
+    solver.sync()
+    return sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+
+
+def _phase_pass(solver, flush, steps: int):
+    """Per-phase milliseconds per step (events between the kernels of each phase)."""
+    import torch
+
+    ext = torch.cuda.ExternalStream(solver.stream)
+    solver.set_phase_timing(True)
+    solver.phase_times(reset=True)
+    for _ in range(steps):
+        with torch.cuda.stream(ext):
+            flush.add_(1)
+        solver.step_async(1)
+    solver.sync()
+    times, n = solver.phase_times(reset=True)
+    solver.set_phase_timing(False)
+    return {k: v / n for k, v in times.items()}
+
+
+def _rel(a, b):
+    nb = float(np.linalg.norm(b))
+    return float(np.linalg.norm(a - b)) / (nb if nb > 0 else 1.0)
+
+
+def run_gpu(args, rank: int, world: int, local_rank: int):
+    import torch
+
+    from sph2d_gb300 import Solver, cases
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    case = cases.piston_flume_2d()
+    p = case.params()
+    flush = torch.zeros(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+
+    # ---- mixed step (headline)
+    sm = Solver(p, "mixed")
+    sm.upload(case.r, case.v, case.rho, case.itype)
+    sm.set_time(0.0)
+    sm.step_async(args.warmup)
+    sm.sync()
+    clocks = ClockSampler(local_rank)
+    launches0 = sm.kernel_launches()
+    _, pairs0 = sm.pair_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ms_mixed = _time_steps(sm, flush, args.steps)
+    clocks_info = clocks.stop()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches = sm.kernel_launches() - launches0
+    last_pairs, pairs1 = sm.pair_count()
+    pairs_timed = pairs1 - pairs0
+    phases_mixed = _phase_pass(sm, flush, min(args.steps, 50))
+
+    # ---- FP64 step beside it
+    steps64 = max(3, min(args.steps, 30))
+    s64 = Solver(p, "fp64")
+    s64.upload(case.r, case.v, case.rho, case.itype)
+    s64.set_time(0.0)
+    s64.step_async(max(2, min(args.warmup, 3)))
+    s64.sync()
+    _, q0 = s64.pair_count()
+    ms_fp64 = _time_steps(s64, flush, steps64)
+    _, q1 = s64.pair_count()
+    phases_fp64 = _phase_pass(s64, flush, min(steps64, 10))
+
+    # ---- error of the mixed step against the FP64 GPU step (same start, same steps)
+    err_steps = 50
+    errors = {}
+    for name, s in (("mixed", sm), ("fp64", s64)):
+        s.upload(case.r, case.v, case.rho, case.itype)
+        s.step(err_steps, 0.0)
+    a, b = sm.download(), s64.download()
+    for k in ("r", "v", "rho", "p"):
+        errors[k] = _rel(a[k], b[k])
+    sm.upload(case.r, case.v, case.rho, case.itype)
+    s64.upload(case.r, case.v, case.rho, case.itype)
+    sm.step(1, 0.0)
+    s64.step(1, 0.0)
+    a, b = sm.download(), s64.download()
+    errors_1 = {k: _rel(a[k], b[k]) for k in ("r", "v", "rho", "p")}
+
+    # ---- end to end through the C ABI with pinned host buffers
+    pin = lambda x: torch.from_numpy(np.ascontiguousarray(x)).pin_memory().numpy()  # noqa: E731
+    hr, hv, hrho, hit = pin(case.r), pin(case.v), pin(case.rho), pin(case.itype)
+    n = case.ntotal
+    out = {k: pin(np.zeros_like(x)) for k, x in (("r", case.r), ("v", case.v), ("rho", case.rho), ("p", case.rho),
+                                                  ("itype", case.itype))}
+    import ctypes as C
+
+    from sph2d_gb300 import capi
+
+    L = capi.lib()
+    dp = lambda x: x.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    ip = lambda x: x.ctypes.data_as(C.POINTER(C.c_int32))  # noqa: E731
+    e2e_steps = max(5, min(args.steps, 40))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        capi.check(L.rrsph_upload(sm.handle, dp(hr), 2, dp(hv), dp(hrho), None, ip(hit)))
+        tt = C.c_double(0.0)
+        capi.check(L.rrsph_step(sm.handle, 1, C.byref(tt)))
+        capi.check(L.rrsph_download(sm.handle, dp(out["r"]), 2, dp(out["v"]), dp(out["rho"]), dp(out["p"]),
+                                    ip(out["itype"])))
+    e2e_s = time.perf_counter() - t0
+    # every e2e step starts from the same uploaded state, so it has the same pairs
+    e2e_pairs = e2e_steps * sm.pair_count()[0]
+    h2d = n * (2 * 8 + 2 * 8 + 8 + 4)
+    d2h = n * (2 * 8 + 2 * 8 + 8 + 8 + 4)
+
+    # ---- aggregate over ranks (max time, summed pairs)
+    t_s = ms_mixed / 1e3
+    tot_pairs = pairs_timed
+    e2e_rate = e2e_pairs / e2e_s
+    if dist:
+        tt = torch.tensor([t_s, e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        pp = torch.tensor([float(pairs_timed), float(e2e_pairs)], device="cuda", dtype=torch.float64)
+        dist.all_reduce(pp, op=dist.ReduceOp.SUM)
+        t_s, e2e_max = float(tt[0]), float(tt[1])
+        tot_pairs, e2e_all = float(pp[0]), float(pp[1])
+        e2e_rate = e2e_all / e2e_max
+    value = tot_pairs / t_s
+
+    fkey = "forces"
+    f_ms = phases_mixed[fkey]
+    bytes_launch = FORCES_MIXED_BYTES_PER_PARTICLE * n
+    achieved = bytes_launch / (f_ms * 1e-3) / 1e9
+    traffic = _profile_traffic()
+    result = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_mixed / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32-pairs/f64-state",
+        "data": "synthetic (seeded flume particles of the workload's shape)",
+        "config": workload_config(case, p, last_pairs),
+        "fp64_step": {
+            "ms_per_step": ms_fp64 / steps64,
+            "pair_interactions_per_s": (q1 - q0) / (ms_fp64 / 1e3),
+            "steps": steps64,
+            "mixed_speedup": (ms_fp64 / steps64) / (ms_mixed / args.steps),
+            "phases_ms_per_step": phases_fp64,
+        },
+        "error_vs_fp64_gpu": {"after_1_step": errors_1, f"after_{err_steps}_steps": errors, "metric": "relative L2"},
+        "phases_ms_per_step": phases_mixed,
+        "roofline": {
+            "bound": "hbm",
+            "kernel": "k_forces_mixed",
+            "achieved": achieved,
+            "peak": hbm_peak,
+            "unit": "GB/s",
+            "frac": achieved / hbm_peak,
+            "peak_source": peak_src,
+            "traffic": traffic,
+            "algorithmic_bytes_per_launch": bytes_launch,
+            "avg_launch_ms": f_ms,
+        },
+        "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "steps": e2e_steps, "path": "rrsph_upload + rrsph_step(1) + rrsph_download, pinned host buffers"},
+        "gpu_launches": launches,
+        "clocks": clocks_info,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(case, p, steps=args.cpu_steps)
+    if dist:
+        dist.destroy_process_group()
+    return result
+
+
+def _profile_traffic():
+    """DRAM bytes per launch of the force kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / "forces_mixed_flume.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch_full_size:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+# ---------------------------------------------------------- CPU arms -------
+
+def cpu_baseline(case, p, steps: int = 3) -> dict:
+    """The CPU oracle (a C restatement of RRSPH_OMP's step) on all host cores,
+    for a bounded sample of the same workload."""
+    from oracle import binding as O
+
+    O.set_threads(os.cpu_count() or 1)
+    O.run(p, case.r, case.v, case.rho, case.itype, nsteps=1)  # warm-up (page-in, OpenMP pool)
+    t0 = time.perf_counter()
+    res = O.run(p, case.r, case.v, case.rho, case.itype, nsteps=steps)
+    dt = time.perf_counter() - t0
+    return {"value": res["pairs"] * steps / dt, "unit": UNIT, "cores": O.threads(), "kind": "port",
+            "sample": f"{steps} full steps of the {case.ntotal}-particle flume (directed pairs of the last step "
+                      f"x steps / wall time), oracle/rrsph_oracle.c with OpenMP",
+            "ms_per_step": dt / steps * 1e3}
+
+
+def run_reference(args, rank: int, world: int) -> dict | None:
+    """The reference's CPU implementation of the step on the host cores: the
+    reference core (oracle/_ref) where it was built, else the C oracle port."""
+    if rank != 0:
+        return None
+    from sph2d_gb300 import build
+
+    build.build_oracle()
+    from oracle import binding as O
+    from sph2d_gb300 import cases
+
+    case = cases.piston_flume_2d()
+    p = case.params()
+    threads = os.cpu_count() or 1
+    steps = max(1, min(args.steps, args.cpu_steps))
+    warm = 1 if args.warmup > 0 else 0
+    if O.ref_available():
+        kind = "reference"
+        if warm:
+            O.ref_run(p, f"run:{warm}", case.r, case.v, case.rho, case.itype, threads=threads)
+        t0 = time.perf_counter()
+        out = O.ref_run(p, f"run:{steps}", case.r, case.v, case.rho, case.itype, threads=threads)
+        wall = time.perf_counter() - t0
+        ms = out["timing"]["total_ms"] / steps
+        pairs = O.run(p, out["r_out"], out["v_out"], out["rho_out"], out["itype_out"], nsteps=1)["pairs"]
+        cores = int(out["timing"]["threads"])
+        del wall
+    else:
+        kind = "port"
+        O.set_threads(threads)
+        if warm:
+            O.run(p, case.r, case.v, case.rho, case.itype, nsteps=warm)
+        t0 = time.perf_counter()
+        res = O.run(p, case.r, case.v, case.rho, case.itype, nsteps=steps)
+        ms = (time.perf_counter() - t0) / steps * 1e3
+        pairs = res["pairs"]
+        cores = O.threads()
+    value = pairs / (ms / 1e3)
+    sample = (f"{steps} full steps of the {case.ntotal}-particle flume on {cores} threads "
+              f"({'reference RRSPH_OMP core built from its sources' if kind == 'reference' else 'C restatement of RRSPH_OMP (oracle)'})")
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded flume particles of the workload's shape)",
+        "config": workload_config(case, p, pairs),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        ap.error("--warmup must be >= 3")
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if "WORLD_SIZE" not in os.environ:
+        world = 1 if args.gpus <= 1 else args.gpus
+        if world > 1:
+            raise SystemExit("for --gpus N > 1 launch with torch.distributed.run (one rank per GPU)")
+    if args.impl == "reference":
+        res = run_reference(args, rank, world)
+    else:
+        import __graft_entry__
+
+        __graft_entry__.build()
+        res = run_gpu(args, rank, world, local_rank)
+    if rank == 0 and res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -215,8 +215,22 @@ int rrsph_download(rrsph_solver* s, double* r, uint32_t stride, double* v,
  * *time_io is the simulation time before the first step and is advanced.
  * The first step after rrsph_upload uses dt/2 for velocities (WholeStep.cpp:33). */
 int rrsph_step(rrsph_solver* s, uint64_t nsteps, double* time_io);
+/* Asynchronous form of rrsph_step: enqueues nsteps steps on the handle's
+ * stream and returns without waiting. The simulation time continues on the
+ * device from the previous step (or from rrsph_set_time). Errors raised by the
+ * device checks are reported by the next rrsph_sync. */
+int rrsph_step_async(rrsph_solver* s, uint64_t nsteps);
+/* Sets the simulation time of the next step (stream-ordered). */
+int rrsph_set_time(rrsph_solver* s, double time);
+/* Waits for the enqueued steps; *time_out (may be NULL) receives the time
+ * after the last step. Returns the status the device checks imply, and clears
+ * the device flags. */
+int rrsph_sync(rrsph_solver* s, double* time_out);
 /* Sticky RRSPH_FLAG_* bits raised by device checks since the last clear. */
 int rrsph_status(rrsph_solver* s, uint32_t* flags, int clear);
+/* Directed neighbour pairs (the entries find_neighbours would list) of the
+ * last completed step, and summed over the steps since rrsph_upload. */
+int rrsph_pair_count(rrsph_solver* s, uint64_t* last_step, uint64_t* total);
 /* Current time step (changes under DT_CORRECTION_DYNAMIC with dt_dynamic_reduce). */
 int rrsph_get_dt(rrsph_solver* s, double* dt);
 

@@ -36,6 +36,7 @@
 #include <cstdlib>
 #include <fstream>
 #include <functional>
+#include <iomanip>
 #include <map>
 #include <sstream>
 #include <string>
@@ -344,6 +345,7 @@ int main(int argc, char** argv) {
             for (size_t i = 0; i < n; i++) it[i] = (int32_t)s.itype(i);
             write_array("itype_out.i32", it.data(), n);
             std::ofstream t(g_dir + "/timing.txt");
+            t << std::setprecision(17);
             int threads_used = 1;
 #ifdef _OPENMP
             threads_used = omp_get_max_threads();

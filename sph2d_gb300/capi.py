@@ -121,8 +121,12 @@ _SIGS = {
     "rrsph_upload": (C.c_int, [C.c_void_p, _dp, C.c_uint32, _dp, _dp, _dp, _i32p]),
     "rrsph_download": (C.c_int, [C.c_void_p, _dp, C.c_uint32, _dp, _dp, _dp, _i32p]),
     "rrsph_step": (C.c_int, [C.c_void_p, C.c_uint64, _dp]),
+    "rrsph_step_async": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "rrsph_set_time": (C.c_int, [C.c_void_p, C.c_double]),
+    "rrsph_sync": (C.c_int, [C.c_void_p, _dp]),
     "rrsph_status": (C.c_int, [C.c_void_p, _u32p, C.c_int]),
     "rrsph_get_dt": (C.c_int, [C.c_void_p, _dp]),
+    "rrsph_pair_count": (C.c_int, [C.c_void_p, _P(C.c_uint64), _P(C.c_uint64)]),
     "rrsph_grid_find": (C.c_int, [C.c_void_p, _u32p, _u32p, _u32p]),
     "rrsph_neighbours": (C.c_int, [C.c_void_p, _u32p, _u32p, C.c_uint32, _P(C.c_uint64)]),
     "rrsph_density": (C.c_int, [C.c_void_p, _dp, _dp]),

@@ -12,6 +12,19 @@ constexpr uint32_t kInvalidCell = 0xFFFFFFFFu;      // GRID_INVALID_CELL (GridUt
 constexpr uint32_t kMaxCellCoord2 = (1u << 16) - 1; // GRID_MAX_CELL_COORD2 (GridUtils.h:9)
 constexpr uint32_t kEmpty = 0xFFFFFFFFu;            // empty cell-table entry
 
+// Float constants of the FP32-mixed gathers, precomputed on the host.
+struct MixedF {
+    float cell, h, inv_h, mass, rho0;
+    float cut2_lo, cut2_hi;     // guard band around the cutoff: pairs inside it are re-tested in double
+    float kf[5];                // kernel factors by skf
+    float w0_density;           // mass * W(0)
+    float lj_rr0, lj_D, etq_h2;
+    float av_alpha_c, av_beta;  // alpha * c, beta
+    float ap_coef, ap_index, ap_inv_wdelta;
+    float avel_coef2;           // 2 * average_velocity_coef
+    float dhc;                  // delta-SPH: coef * h * c
+};
+
 // Everything a kernel needs from rrsph_params, precomputed on the host.
 struct DevParams {
     int dim;
@@ -53,6 +66,8 @@ struct DevParams {
     int dt_method;          // 0 const, 1 CFL const, 2 dynamic
     int dt_reduce;          // 1: true max reduction
     double cfl, never_ending_dt;
+    int all_cubic;          // every smoothing kernel choice is the cubic spline
+    MixedF mf;
 };
 
 // Per-step scalars kept on the device (double-buffered by step parity so a
@@ -63,8 +78,9 @@ struct StepScalars {
     unsigned long long step;   // itimestep of the reference loop
     unsigned long long amax_bits;  // max |a| over particles (as ordered bits)
     unsigned long long mumax_bits; // max arvmu
-    unsigned long long pairs;      // directed pairs found by the density gather
-    unsigned long long pad[2];
+    unsigned long long pairs;      // directed pairs found by the density gather of this step
+    unsigned long long nwm_off;    // 1 once a one-shot wave maker (wall disappear) has fired
+    unsigned long long pairs_total;  // pairs summed over the steps since upload
 };
 
 // ---------------------------------------------------------------- Morton --

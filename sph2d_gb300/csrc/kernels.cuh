@@ -39,8 +39,8 @@ struct Sorted {
     // FP32-mixed gathers
     float4* P4;    // cell-relative position (x, y, z) + itype bits
     float4* V4;    // velocity the forces use + density the forces use
-    float4* VD4;   // v + rho for density_con
-    float* pf;     // pressure
+    float4* VD4;   // v + (rho - rho0) for density_con
+    float2* PR;    // pressure p and p / rho^2 (rho = the density the forces use)
 };
 
 // Sources the reorder gathers for the force velocity / density.

@@ -90,10 +90,10 @@ __global__ void k_reorder(DevParams P, State S, Sorted G, GatherSrc F, int mixed
         const float oz = DIM == 3 ? (float)(z - (P.zmin + (double)cz * P.cell)) : 0.0f;
         G.P4[k] = make_float4(ox, oy, oz, __int_as_float(t));
         G.V4[k] = make_float4((float)fvx, (float)fvy, (float)fvz, (float)frho);
-        if (F.p) G.pf[k] = (float)F.p[id];
-        if (cont)
+        if (F.p) G.PR[k] = make_float2((float)F.p[id], (float)(F.p[id] / (frho * frho)));
+        if (cont)  // the density deviation keeps rho_i - rho_j accurate in float
             G.VD4[k] = make_float4((float)S.vx[id], (float)S.vy[id], DIM == 3 ? (float)S.vz[id] : 0.0f,
-                                   (float)S.rho[id]);
+                                   (float)(S.rho[id] - P.rho0));
     }
 }
 
@@ -149,7 +149,7 @@ __global__ void k_whole(DevParams P, State S, const StepScalars* __restrict__ sc
         if (dt <= P.never_ending_dt && i == 0) atomicOr(flags, RRSPH_FLAG_NEVER_ENDING);
     }
     const double time = scal->time;
-    const unsigned long long nwm_off = scal->pad[0];
+    const unsigned long long nwm_off = scal->nwm_off;
     if (i == 0) {
         next->time = time + dt;
         next->dt = dt;
@@ -157,8 +157,8 @@ __global__ void k_whole(DevParams P, State S, const StepScalars* __restrict__ sc
         next->amax_bits = 0;
         next->mumax_bits = 0;
         next->pairs = 0;
-        next->pad[0] = nwm_off || (P.nwm == 4 && time >= P.nwm_time_start) ? 1ull : 0ull;
-        next->pad[1] = 0;
+        next->nwm_off = nwm_off || (P.nwm == 4 && time >= P.nwm_time_start) ? 1ull : 0ull;
+        next->pairs_total = scal->pairs_total + scal->pairs;
     }
     if (i >= P.n) return;
     const bool waves = P.nwm && !nwm_off && time >= P.nwm_time_start;

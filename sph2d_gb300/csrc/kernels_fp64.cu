@@ -46,10 +46,17 @@ __global__ void __launch_bounds__(kGatherThreads) k_density(DevParams P, State S
         const double f = P.kf[skf];
         double acc = cont ? 0.0 : P.mass * P.w0_density;
         if (G.itype[k] != P.type_non_existent) {
-            for_neighbour_cells<DIM>(P, G.key[k], [&](uint32_t c, int, int, int) {
-                const uint32_t s = G.cell_start[c];
-                if (s == kEmpty) return;
-                const uint32_t e = G.cell_end[c];
+            uint64_t cx, cy, cz;
+            decode_key<DIM>(G.key[k], cx, cy, cz);
+            constexpr int NC = DIM == 3 ? 27 : 9;
+#pragma unroll 1
+            for (int c = 0; c < NC; c++) {
+                uint32_t cell;
+                int sx, sy, sz;
+                if (!stencil_cell<DIM>(P, cx, cy, cz, c, cell, sx, sy, sz)) continue;
+                const uint32_t s = G.cell_start[cell];
+                if (s == kEmpty) continue;
+                const uint32_t e = G.cell_end[cell];
                 for (uint32_t i = s; i < e; i++) {
                     if (i == k || G.itype[i] == P.type_non_existent) continue;
                     const double dx = __dsub_rn(G.rx[i], xj), dy = __dsub_rn(G.ry[i], yj);
@@ -79,7 +86,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_density(DevParams P, State S
                         }
                     }
                 }
-            });
+            }
         }
         if (cnt > P.max_nb - 1) atomicOr(flags, RRSPH_FLAG_NEIGHBOUR_OVERFLOW);
         if (!cont) {
@@ -123,10 +130,17 @@ __global__ void __launch_bounds__(kGatherThreads) k_forces(DevParams P, State S,
         const bool avel = (terms & RRSPH_TERM_AVERAGE_VELOCITY) && P.avg_vel;
         const double pj_r2 = pj / (rhoj * rhoj);
         if (tj != P.type_non_existent) {
-            for_neighbour_cells<DIM>(P, G.key[k], [&](uint32_t c, int, int, int) {
-                const uint32_t s = G.cell_start[c];
-                if (s == kEmpty) return;
-                const uint32_t e = G.cell_end[c];
+            uint64_t cx, cy, cz;
+            decode_key<DIM>(G.key[k], cx, cy, cz);
+            constexpr int NC = DIM == 3 ? 27 : 9;
+#pragma unroll 1
+            for (int c = 0; c < NC; c++) {
+                uint32_t cell;
+                int sx, sy, sz;
+                if (!stencil_cell<DIM>(P, cx, cy, cz, c, cell, sx, sy, sz)) continue;
+                const uint32_t s = G.cell_start[cell];
+                if (s == kEmpty) continue;
+                const uint32_t e = G.cell_end[cell];
                 for (uint32_t i = s; i < e; i++) {
                     if (i == k) continue;
                     const int32_t ti = G.itype[i];
@@ -188,7 +202,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_forces(DevParams P, State S,
                         }
                     }
                 }
-            });
+            }
         }
         S.ax[id] = ax;
         S.ay[id] = ay;

@@ -6,8 +6,12 @@
 // keeps ~1e-7 relative accuracy of h anywhere in the domain. Pairs whose float
 // distance lies within a guard band of the cutoff are re-tested with the
 // reference's double arithmetic, so the neighbour set equals the FP64 one.
-// Density and force sums are Kahan-compensated; the per-particle EOS and all
-// state updates stay in double.
+// Sums are accumulated per neighbour cell in float and Kahan-compensated across
+// cells; the per-particle EOS and all state updates stay in double.
+//
+// One thread per particle in cell order. The 3^dim stencil is a runtime loop
+// (a single copy of the pair body keeps the kernel in the instruction cache);
+// reciprocals and square roots use the fast MUFU forms (<= 2 ulp).
 #include "kernels.cuh"
 #include "neighbour.cuh"
 
@@ -26,9 +30,10 @@ struct Kahan {
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
+// W(q) of smoothing kernel skf (SmoothingKernel.h:20-252), float.
 __device__ __forceinline__ float kernel_wf(int skf, float f, float q) {
     switch (skf) {
-    case 2: return f * expf(-q * q);
+    case 2: return f * __expf(-q * q);
     case 3: {
         if (q <= 2.0f) {
             const float t = 1.0f - 0.5f * q;
@@ -48,10 +53,10 @@ __device__ __forceinline__ float kernel_wf(int skf, float f, float q) {
     }
 }
 
-// dW/dr = diff * scale (diff = r_i - r_j)
+// dW/dr = diff * scale with diff = r_i - r_j (SmoothingKernel.h:42-274), float.
 __device__ __forceinline__ float kernel_dwdr_scalef(int skf, float f, float q, float inv_dist, float inv_h) {
     switch (skf) {
-    case 2: return inv_h * inv_h * (-2.0f) * (f * expf(-q * q));
+    case 2: return inv_h * inv_h * (-2.0f) * (f * __expf(-q * q));
     case 3: {
         if (q < 1.e-6f || !(q < 2.0f)) return 0.0f;
         const float t = 1.0f - 0.5f * q;
@@ -69,30 +74,11 @@ __device__ __forceinline__ float kernel_dwdr_scalef(int skf, float f, float q, f
     }
 }
 
-struct MixedConsts {
-    float cell, inv_h, h, mass, cut2_lo, cut2_hi;
-    float kf[5];
-};
-
-__device__ __forceinline__ MixedConsts mixed_consts(const DevParams& P) {
-    MixedConsts M;
-    M.cell = (float)P.cell;
-    M.inv_h = (float)P.inv_h;
-    M.h = (float)P.h;
-    M.mass = (float)P.mass;
-    M.cut2_lo = (float)(P.cut2 * (1.0 - 1e-5));
-    M.cut2_hi = (float)(P.cut2 * (1.0 + 1e-5));
-#pragma unroll
-    for (int s = 0; s < 5; s++) M.kf[s] = (float)P.kf[s];
-    return M;
-}
-
-// Cutoff test with the double re-test inside the guard band.
+// Cutoff test: float test outside the guard band, the reference's double test inside it.
 template <int DIM>
-__device__ __forceinline__ bool within_cutoff(const DevParams& P, const MixedConsts& M, const Sorted& G, uint32_t i,
-                                              uint32_t k, float d2) {
-    if (d2 >= M.cut2_hi) return false;
-    if (d2 < M.cut2_lo) return true;
+__device__ __forceinline__ bool within_cutoff(const DevParams& P, const Sorted& G, uint32_t i, uint32_t k, float d2) {
+    if (d2 >= P.mf.cut2_hi) return false;
+    if (d2 < P.mf.cut2_lo) return true;
     const double dx = __dsub_rn(G.rx[i], G.rx[k]), dy = __dsub_rn(G.ry[i], G.ry[k]);
     const double dz = DIM == 3 ? __dsub_rn(G.rz[i], G.rz[k]) : 0.0;
     return exact_dist2<DIM>(dx, dy, dz) < P.cut2;
@@ -109,7 +95,9 @@ __device__ __forceinline__ void warp_max_bits(unsigned long long* dst, double v)
     if ((threadIdx.x & 31) == 0 && v > 0) atomicMax(dst, dbits(v));
 }
 
-template <int DIM>
+// density_sum / density_con (Density.h:25-114) + EOS. SKF: 1 = cubic only
+// (every kernel choice cubic), 0 = any kernel (runtime switch).
+template <int DIM, int SKF>
 __global__ void __launch_bounds__(kGatherThreads) k_density_mixed(DevParams P, State S, Sorted G,
                                                                   StepScalars* __restrict__ scal,
                                                                   uint32_t* __restrict__ flags) {
@@ -117,64 +105,75 @@ __global__ void __launch_bounds__(kGatherThreads) k_density_mixed(DevParams P, S
     const bool active = k < P.n;
     uint32_t cnt = 0;
     if (active) {
-        const MixedConsts M = mixed_consts(P);
+        const MixedF& M = P.mf;
         const uint32_t id = G.id[k];
         const bool cont = P.density_treatment != 0;
+        const bool delta = P.density_treatment == 2;
         const float4 pj = G.P4[k];
         const int32_t tj = __float_as_int(pj.w);
         float4 vdj = make_float4(0, 0, 0, 0);
         if (cont) vdj = G.VD4[k];
-        const int skf = P.density_skf;
+        const int skf = SKF ? SKF : P.density_skf;
         const float f = M.kf[skf];
-        const float dhc = (float)P.delta_sph_dhc;
         Kahan acc{0.0f, 0.0f};
         if (tj != P.type_non_existent) {
-            for_neighbour_cells<DIM>(P, G.key[k], [&](uint32_t c, int sx, int sy, int sz) {
-                const uint32_t s = G.cell_start[c];
-                if (s == kEmpty) return;
-                const uint32_t e = G.cell_end[c];
+            uint64_t cx, cy, cz;
+            decode_key<DIM>(G.key[k], cx, cy, cz);
+            constexpr int NC = DIM == 3 ? 27 : 9;
+#pragma unroll 1
+            for (int c = 0; c < NC; c++) {
+                uint32_t cell;
+                int sx, sy, sz;
+                if (!stencil_cell<DIM>(P, cx, cy, cz, c, cell, sx, sy, sz)) continue;
+                const uint32_t s = G.cell_start[cell];
+                if (s == kEmpty) continue;
+                const uint32_t e = G.cell_end[cell];
                 const float shx = (float)sx * M.cell - pj.x;
                 const float shy = (float)sy * M.cell - pj.y;
                 const float shz = DIM == 3 ? (float)sz * M.cell - pj.z : 0.0f;
+                float part = 0.0f;
                 for (uint32_t i = s; i < e; i++) {
                     if (i == k) continue;
                     const float4 pi = G.P4[i];
                     if (__float_as_int(pi.w) == P.type_non_existent) continue;
                     const float dx = pi.x + shx, dy = pi.y + shy, dz = DIM == 3 ? pi.z + shz : 0.0f;
                     const float d2 = DIM == 3 ? dx * dx + dy * dy + dz * dz : dx * dx + dy * dy;
-                    if (!within_cutoff<DIM>(P, M, G, i, k, d2)) continue;
+                    if (!within_cutoff<DIM>(P, G, i, k, d2)) continue;
                     cnt++;
-                    const float dist = sqrtf(d2);
-                    const float q = dist * M.inv_h;
+                    const float inv_dist = rsqrtf(d2);
+                    const float q = d2 * inv_dist * M.inv_h;
                     if (!cont) {
-                        acc.add(M.mass * kernel_wf(skf, f, q));
+                        part += kernel_wf(skf, f, q);
                     } else {
-                        const float sc = kernel_dwdr_scalef(skf, f, q, 1.0f / dist, M.inv_h);
+                        const float sc = kernel_dwdr_scalef(skf, f, q, inv_dist, M.inv_h);
                         const float4 vdi = G.VD4[i];
                         float vcc = (vdi.x - vdj.x) * dx + (vdi.y - vdj.y) * dy;
                         if (DIM == 3) vcc += (vdi.z - vdj.z) * dz;
-                        float term = M.mass * (vcc * sc);
-                        if (P.density_treatment == 2) {
-                            const float r_factor = -sc;  // dot(r_j - r_i, diff * sc) / |diff|^2
-                            const float rho_factor = (vdi.w - vdj.w) / vdi.w;
-                            term += 2.0f * dhc * (rho_factor * r_factor) * M.mass;
+                        float term = vcc * sc;
+                        if (delta) {
+                            // r_factor = dot(r_j - r_i, diff * sc) / |diff|^2 = -sc;
+                            // rho_factor = (rho_i - rho_j) / rho_i on the deviations from rho0
+                            const float rho_factor = __fdividef(vdi.w - vdj.w, M.rho0 + vdi.w);
+                            term += 2.0f * M.dhc * (rho_factor * -sc);
                         }
-                        acc.add(term);
+                        part += term;
                     }
                 }
-            });
+                acc.add(M.mass * part);
+            }
         }
         if (cnt > P.max_nb - 1) atomicOr(flags, RRSPH_FLAG_NEIGHBOUR_OVERFLOW);
         if (!cont) {
-            const double rho = (double)(M.mass * kernel_wf(skf, f, 0.0f)) + acc.value();
+            const double rho = (double)M.w0_density + acc.value();
             const double pr = eos_p(P, rho);
             G.V4[k].w = (float)rho;
-            G.pf[k] = (float)pr;
+            G.PR[k] = make_float2((float)pr, (float)(pr / (rho * rho)));
             S.rho[id] = rho;
             S.p[id] = pr;
         } else {
             const double pr = eos_p(P, S.rho[id]);
-            G.pf[k] = (float)pr;
+            const double rf = (double)G.V4[k].w;  // rho_predict, the density of the forces
+            G.PR[k] = make_float2((float)pr, (float)(pr / (rf * rf)));
             S.p[id] = pr;
             S.drho[id] = acc.value();
         }
@@ -182,7 +181,9 @@ __global__ void __launch_bounds__(kGatherThreads) k_density_mixed(DevParams P, S
     warp_sum_add(&scal->pairs, cnt);
 }
 
-template <int DIM>
+// update_acceleration (UpdateAcceleration.cpp:33-125) with the external
+// (Lennard-Jones), internal (pressure), artificial-viscosity and XSPH terms.
+template <int DIM, int SKF>
 __global__ void __launch_bounds__(kGatherThreads) k_forces_mixed(DevParams P, State S, Sorted G, uint32_t terms,
                                                                  StepScalars* __restrict__ scal,
                                                                  uint32_t* __restrict__ flags, int write_mu) {
@@ -190,11 +191,12 @@ __global__ void __launch_bounds__(kGatherThreads) k_forces_mixed(DevParams P, St
     const bool active = k < P.n;
     double amag = 0, arvmu_d = 0;
     if (active) {
-        const MixedConsts M = mixed_consts(P);
+        const MixedF& M = P.mf;
         const uint32_t id = G.id[k];
         const float4 pj4 = G.P4[k];
         const float4 vj = G.V4[k];
-        const float rhoj = vj.w, pj = G.pf[k];
+        const float2 prj = G.PR[k];
+        const float rhoj = vj.w;
         const int32_t tj = __float_as_int(pj4.w);
         Kahan ax{0, 0}, ay{0, 0}, az{0, 0};
         Kahan avx{0, 0}, avy{0, 0}, avz{0, 0};
@@ -203,20 +205,25 @@ __global__ void __launch_bounds__(kGatherThreads) k_forces_mixed(DevParams P, St
         const bool intf = terms & RRSPH_TERM_INTERNAL;
         const bool visc = (terms & RRSPH_TERM_ART_VISC) && P.art_visc;
         const bool avel = (terms & RRSPH_TERM_AVERAGE_VELOCITY) && P.avg_vel;
-        const float pj_r2 = pj / (rhoj * rhoj);
-        const float rr0 = (float)P.lj_rr0, lj_D = (float)P.lj_D;
-        const float etq_h2 = (float)P.etq_h2;
-        const float av_alpha_c = (float)(P.av_alpha * P.c_av), av_beta = (float)P.av_beta;
-        const float ap_coef = (float)P.ap_coef, ap_index = (float)P.ap_index, ap_inv_wdelta = (float)(1.0 / P.ap_wdelta);
-        const float avel_coef2 = (float)(2.0 * P.avg_vel_coef);
+        const bool form1 = P.intf_form == 1;
+        const int intf_skf = SKF ? SKF : P.intf_skf;
+        const int av_skf = SKF ? SKF : P.av_skf;
         if (tj != P.type_non_existent) {
-            for_neighbour_cells<DIM>(P, G.key[k], [&](uint32_t c, int sx, int sy, int sz) {
-                const uint32_t s = G.cell_start[c];
-                if (s == kEmpty) return;
-                const uint32_t e = G.cell_end[c];
+            uint64_t cx, cy, cz;
+            decode_key<DIM>(G.key[k], cx, cy, cz);
+            constexpr int NC = DIM == 3 ? 27 : 9;
+#pragma unroll 1
+            for (int c = 0; c < NC; c++) {
+                uint32_t cell;
+                int sx, sy, sz;
+                if (!stencil_cell<DIM>(P, cx, cy, cz, c, cell, sx, sy, sz)) continue;
+                const uint32_t s = G.cell_start[cell];
+                if (s == kEmpty) continue;
+                const uint32_t e = G.cell_end[cell];
                 const float shx = (float)sx * M.cell - pj4.x;
                 const float shy = (float)sy * M.cell - pj4.y;
                 const float shz = DIM == 3 ? (float)sz * M.cell - pj4.z : 0.0f;
+                float cax = 0.0f, cay = 0.0f, caz = 0.0f, cvx = 0.0f, cvy = 0.0f, cvz = 0.0f;
                 for (uint32_t i = s; i < e; i++) {
                     if (i == k) continue;
                     const float4 pi4 = G.P4[i];
@@ -224,27 +231,27 @@ __global__ void __launch_bounds__(kGatherThreads) k_forces_mixed(DevParams P, St
                     if (ti == P.type_non_existent) continue;
                     const float dx = pi4.x + shx, dy = pi4.y + shy, dz = DIM == 3 ? pi4.z + shz : 0.0f;
                     const float d2 = DIM == 3 ? dx * dx + dy * dy + dz * dz : dx * dx + dy * dy;
-                    if (!within_cutoff<DIM>(P, M, G, i, k, d2)) continue;
-                    const float dist = sqrtf(d2);
-                    const float inv_dist = 1.0f / dist;
+                    if (!within_cutoff<DIM>(P, G, i, k, d2)) continue;
+                    const float inv_dist = rsqrtf(d2);
+                    const float dist = d2 * inv_dist;
                     const float q = dist * M.inv_h;
                     float m = 0.0f;  // coefficient of diff (= r_i - r_j) in this pair's acceleration
-                    if (ext && ti < 0 && dist < rr0) {
-                        const float rn = rr0 * inv_dist;
+                    if (ext && ti < 0 && dist < M.lj_rr0) {
+                        const float rn = M.lj_rr0 * inv_dist;
                         const float rn2 = rn * rn, rn4 = rn2 * rn2, rn8 = rn4 * rn4;
-                        m -= lj_D * (rn8 * rn4 - rn4) / d2;
+                        m -= M.lj_D * (rn8 * rn4 - rn4) * (inv_dist * inv_dist);
                     }
                     const float4 vi = G.V4[i];
                     const float rhoi = vi.w;
+                    const float sc = kernel_dwdr_scalef(intf_skf, M.kf[intf_skf], q, inv_dist, M.inv_h);
                     if (intf) {
-                        const float pi = G.pf[i];
-                        const float sc = kernel_dwdr_scalef(P.intf_skf, M.kf[P.intf_skf], q, inv_dist, M.inv_h);
-                        float pf = P.intf_form == 1 ? (pj + pi) / (rhoj * rhoi) : (pi / (rhoi * rhoi) + pj_r2);
-                        if (P.art_pressure && (pi < 0 || pj < 0)) {
+                        const float2 pri = G.PR[i];
+                        float pf = form1 ? __fdividef(prj.x + pri.x, rhoj * rhoi) : (pri.y + prj.y);
+                        if (P.art_pressure && (pri.x < 0 || prj.x < 0)) {
                             const float w = kernel_wf(P.ap_skf, M.kf[P.ap_skf], q);
-                            const float api = pi < 0 ? (-ap_coef * pi / (rhoi * rhoi)) : 0.0f;
-                            const float apj = pj < 0 ? (-ap_coef * pj / (rhoj * rhoj)) : 0.0f;
-                            pf += (api + apj) * powf(w * ap_inv_wdelta, ap_index);
+                            const float api = pri.x < 0 ? (-M.ap_coef * pri.y) : 0.0f;
+                            const float apj = prj.x < 0 ? (-M.ap_coef * prj.y) : 0.0f;
+                            pf += (api + apj) * __powf(w * M.ap_inv_wdelta, M.ap_index);
                         }
                         m += sc * pf * M.mass;
                     }
@@ -252,26 +259,35 @@ __global__ void __launch_bounds__(kGatherThreads) k_forces_mixed(DevParams P, St
                         float vr = -((vj.x - vi.x) * dx + (vj.y - vi.y) * dy);
                         if (DIM == 3) vr -= (vj.z - vi.z) * dz;
                         if (vr < 0) {
-                            const float mu = M.h * vr / (d2 + etq_h2);
+                            const float mu = __fdividef(M.h * vr, d2 + M.etq_h2);
                             arvmu = fmaxf(arvmu, fabsf(mu));
-                            const float rho_ij = 0.5f * (rhoi + rhoj);
-                            const float piv = (av_beta * mu - av_alpha_c) * mu / rho_ij;
-                            const float sc = kernel_dwdr_scalef(P.av_skf, M.kf[P.av_skf], q, inv_dist, M.inv_h);
-                            m += sc * piv * M.mass;
+                            const float piv = __fdividef((M.av_beta * mu - M.av_alpha_c) * mu, 0.5f * (rhoi + rhoj));
+                            const float sca = (SKF || av_skf == intf_skf)
+                                                  ? sc
+                                                  : kernel_dwdr_scalef(av_skf, M.kf[av_skf], q, inv_dist, M.inv_h);
+                            m += sca * piv * M.mass;
                         }
                     }
-                    ax.add(dx * m);
-                    ay.add(dy * m);
-                    if (DIM == 3) az.add(dz * m);
+                    cax += dx * m;
+                    cay += dy * m;
+                    if (DIM == 3) caz += dz * m;
                     if (avel && ti > 0) {
-                        const float w = kernel_wf(P.avel_skf, M.kf[P.avel_skf], q);
-                        const float mv = M.mass / (rhoi + rhoj) * w * avel_coef2;
-                        avx.add((vi.x - vj.x) * mv);
-                        avy.add((vi.y - vj.y) * mv);
-                        if (DIM == 3) avz.add((vi.z - vj.z) * mv);
+                        const float w = kernel_wf(SKF ? SKF : P.avel_skf, M.kf[SKF ? SKF : P.avel_skf], q);
+                        const float mv = __fdividef(M.mass * w * M.avel_coef2, rhoi + rhoj);
+                        cvx += (vi.x - vj.x) * mv;
+                        cvy += (vi.y - vj.y) * mv;
+                        if (DIM == 3) cvz += (vi.z - vj.z) * mv;
                     }
                 }
-            });
+                ax.add(cax);
+                ay.add(cay);
+                if (DIM == 3) az.add(caz);
+                if (avel) {
+                    avx.add(cvx);
+                    avy.add(cvy);
+                    if (DIM == 3) avz.add(cvz);
+                }
+            }
         }
         const double g = (terms & RRSPH_TERM_GRAVITY) ? P.g : 0.0;
         const double axd = ax.value(), ayd = ay.value() - g, azd = DIM == 3 ? az.value() : 0.0;
@@ -285,7 +301,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_forces_mixed(DevParams P, St
         }
         arvmu_d = arvmu;
         if (write_mu) S.mu[id] = arvmu_d;
-        amag = sqrt(axd * axd + ayd * ayd + azd * azd);
+        if (P.dt_reduce) amag = sqrt(axd * axd + ayd * ayd + azd * azd);
     }
     if (P.dt_method == 2 && P.dt_reduce) {
         warp_max_bits(&scal->amax_bits, amag);
@@ -298,14 +314,16 @@ __global__ void __launch_bounds__(kGatherThreads) k_forces_mixed(DevParams P, St
 template <int DIM>
 void launch_density_mixed(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
                           cudaStream_t st) {
-    k_density_mixed<DIM><<<(P.n + kGatherThreads - 1) / kGatherThreads, kGatherThreads, 0, st>>>(P, S, G, scal,
-                                                                                                  flags);
+    const unsigned blocks = (P.n + kGatherThreads - 1) / kGatherThreads;
+    if (P.all_cubic) k_density_mixed<DIM, 1><<<blocks, kGatherThreads, 0, st>>>(P, S, G, scal, flags);
+    else k_density_mixed<DIM, 0><<<blocks, kGatherThreads, 0, st>>>(P, S, G, scal, flags);
 }
 template <int DIM>
 void launch_forces_mixed(const DevParams& P, const State& S, const Sorted& G, uint32_t terms, StepScalars* scal,
                          uint32_t* flags, int write_mu, cudaStream_t st) {
-    k_forces_mixed<DIM><<<(P.n + kGatherThreads - 1) / kGatherThreads, kGatherThreads, 0, st>>>(P, S, G, terms, scal,
-                                                                                                 flags, write_mu);
+    const unsigned blocks = (P.n + kGatherThreads - 1) / kGatherThreads;
+    if (P.all_cubic) k_forces_mixed<DIM, 1><<<blocks, kGatherThreads, 0, st>>>(P, S, G, terms, scal, flags, write_mu);
+    else k_forces_mixed<DIM, 0><<<blocks, kGatherThreads, 0, st>>>(P, S, G, terms, scal, flags, write_mu);
 }
 
 template void launch_density_mixed<2>(const DevParams&, const State&, const Sorted&, StepScalars*, uint32_t*,

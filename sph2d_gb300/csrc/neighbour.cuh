@@ -57,6 +57,43 @@ __device__ __forceinline__ void for_neighbour_cells(const DevParams& P, uint32_t
     }
 }
 
+// The c-th cell (c in [0, 3^DIM)) of the stencil of the cell at (cx, cy, cz),
+// in the order of get_neighbouring_cells2/3 (x outer, then y, then z). Returns
+// false when the reference marks the cell invalid or its key is >= max_cells.
+// (sx, sy, sz) is the displacement of the cell's coordinates from the centre.
+template <int DIM>
+__device__ __forceinline__ bool stencil_cell(const DevParams& P, uint64_t cx, uint64_t cy, uint64_t cz, int c,
+                                             uint32_t& cell, int& sx, int& sy, int& sz) {
+    int dx, dy, dz;
+    if (DIM == 3) {
+        dx = c / 9 - 1;
+        dy = (c / 3) % 3 - 1;
+        dz = c % 3 - 1;
+    } else {
+        dx = c / 3 - 1;
+        dy = c % 3 - 1;
+        dz = 0;
+    }
+    const uint64_t x = step_coord(cx, dx), y = step_coord(cy, dy);
+    if (x == kInvalidCell || y == kInvalidCell) return false;
+    uint64_t key;
+    const uint64_t mask = DIM == 3 ? 0x3FFull : 0xFFFFull;
+    if (DIM == 3) {
+        const uint64_t z = step_coord(cz, dz);
+        if (z == kInvalidCell) return false;
+        key = split3(x) | (split3(y) << 1) | (split3(z) << 2);
+        sz = (int)((int64_t)(z & mask) - (int64_t)cz);
+    } else {
+        key = split2(x) | (split2(y) << 1);
+        sz = 0;
+    }
+    if (key >= P.max_cells) return false;
+    cell = (uint32_t)key;
+    sx = (int)((int64_t)(x & mask) - (int64_t)cx);
+    sy = (int)((int64_t)(y & mask) - (int64_t)cy);
+    return true;
+}
+
 // The reference's cutoff test dist^2 < (cell_scale_k*h)^2 (GridFind.cpp:143-146)
 // in double without contraction, so the pair set matches bit for bit.
 template <int DIM>

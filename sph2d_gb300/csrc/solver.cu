@@ -171,6 +171,27 @@ int fill_dev_params(const rrsph_params& p, rrsph::DevParams& P) {
     P.dt_reduce = p.dt_dynamic_reduce ? 1 : 0;
     P.cfl = p.CFL_coef;
     P.never_ending_dt = (p.hsml / P.c_eos) * 1.E-6;
+    P.all_cubic = P.density_skf == 1 && P.intf_skf == 1 && P.av_skf == 1 && P.avel_skf == 1 && P.ap_skf == 1;
+    rrsph::MixedF& M = P.mf;
+    M.cell = (float)P.cell;
+    M.h = (float)P.h;
+    M.inv_h = (float)P.inv_h;
+    M.mass = (float)P.mass;
+    M.rho0 = (float)P.rho0;
+    M.cut2_lo = (float)(P.cut2 * (1.0 - 1e-5));
+    M.cut2_hi = (float)(P.cut2 * (1.0 + 1e-5));
+    for (int k = 0; k < 5; k++) M.kf[k] = (float)P.kf[k];
+    M.w0_density = (float)(P.mass * P.w0_density);
+    M.lj_rr0 = (float)P.lj_rr0;
+    M.lj_D = (float)P.lj_D;
+    M.etq_h2 = (float)P.etq_h2;
+    M.av_alpha_c = (float)(P.av_alpha * P.c_av);
+    M.av_beta = (float)P.av_beta;
+    M.ap_coef = (float)P.ap_coef;
+    M.ap_index = (float)P.ap_index;
+    M.ap_inv_wdelta = (float)(1.0 / P.ap_wdelta);
+    M.avel_coef2 = (float)(2.0 * P.avg_vel_coef);
+    M.dhc = (float)P.delta_sph_dhc;
     return RRSPH_OK;
 }
 
@@ -321,7 +342,7 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
         A(G.rho, n); A(G.p, n);
         if (cont) { A(G.vdx, n); A(G.vdy, n); if (d3) A(G.vdz, n); A(G.rhod, n); }
     } else {
-        A(G.P4, n); A(G.V4, n); A(G.pf, n);
+        A(G.P4, n); A(G.V4, n); A(G.PR, n);
         if (cont) A(G.VD4, n);
     }
     A(s->scal, 2);
@@ -429,15 +450,10 @@ extern "C" int rrsph_download(rrsph_solver* s, double* r, uint32_t stride, doubl
     return RRSPH_OK;
 }
 
-extern "C" int rrsph_step(rrsph_solver* s, uint64_t nsteps, double* time_io) {
-    int rc = check_handle(s, "rrsph_step");
-    if (rc) return rc;
-    if (!time_io) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_step: null time");
+namespace {
+
+int enqueue_steps(rrsph_solver* s, uint64_t nsteps) {
     cudaStream_t st = s->stream;
-    const int par0 = (int)(s->step_index & 1);
-    *s->h_time = *time_io;
-    RRSPH_CUDA_TRY(cudaMemcpyAsync(&s->scal[par0].time, s->h_time, sizeof(double), cudaMemcpyHostToDevice, st));
-    RRSPH_CUDA_TRY(cudaMemsetAsync(s->flags, 0, sizeof(uint32_t), st));
     for (uint64_t k = 0; k < nsteps; k++) {
         const int par = (int)(s->step_index & 1);
         if (s->timing) {
@@ -469,13 +485,50 @@ extern "C" int rrsph_step(rrsph_solver* s, uint64_t nsteps, double* time_io) {
         }
         s->step_index++;
     }
+    return RRSPH_OK;
+}
+
+}  // namespace
+
+extern "C" int rrsph_set_time(rrsph_solver* s, double time) {
+    int rc = check_handle(s, "rrsph_set_time");
+    if (rc) return rc;
+    // the pinned staging word may still be read by an earlier copy
+    RRSPH_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    *s->h_time = time;
+    const int par = (int)(s->step_index & 1);
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(&s->scal[par].time, s->h_time, sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    return RRSPH_OK;
+}
+
+extern "C" int rrsph_step_async(rrsph_solver* s, uint64_t nsteps) {
+    int rc = check_handle(s, "rrsph_step_async");
+    if (rc) return rc;
+    return enqueue_steps(s, nsteps);
+}
+
+extern "C" int rrsph_sync(rrsph_solver* s, double* time_out) {
+    int rc = check_handle(s, "rrsph_sync");
+    if (rc) return rc;
+    cudaStream_t st = s->stream;
     const int parn = (int)(s->step_index & 1);
     RRSPH_CUDA_TRY(cudaMemcpyAsync(s->h_scal, &s->scal[parn], sizeof(rrsph::StepScalars), cudaMemcpyDeviceToHost, st));
     RRSPH_CUDA_TRY(cudaMemcpyAsync(s->h_flags, s->flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    RRSPH_CUDA_TRY(cudaMemsetAsync(s->flags, 0, sizeof(uint32_t), st));
     RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
     RRSPH_CUDA_TRY(cudaGetLastError());
-    *time_io = s->h_scal->time;
+    if (time_out) *time_out = s->h_scal->time;
     return flags_to_status(s, *s->h_flags);
+}
+
+extern "C" int rrsph_step(rrsph_solver* s, uint64_t nsteps, double* time_io) {
+    int rc = check_handle(s, "rrsph_step");
+    if (rc) return rc;
+    if (!time_io) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_step: null time");
+    if ((rc = rrsph_set_time(s, *time_io)) != 0) return rc;
+    RRSPH_CUDA_TRY(cudaMemsetAsync(s->flags, 0, sizeof(uint32_t), s->stream));
+    if ((rc = enqueue_steps(s, nsteps)) != 0) return rc;
+    return rrsph_sync(s, time_io);
 }
 
 extern "C" int rrsph_status(rrsph_solver* s, uint32_t* flags, int clear) {
@@ -486,6 +539,22 @@ extern "C" int rrsph_status(rrsph_solver* s, uint32_t* flags, int clear) {
     if (clear) RRSPH_CUDA_TRY(cudaMemsetAsync(s->flags, 0, sizeof(uint32_t), s->stream));
     RRSPH_CUDA_TRY(cudaStreamSynchronize(s->stream));
     *flags = *s->h_flags;
+    return RRSPH_OK;
+}
+
+extern "C" int rrsph_pair_count(rrsph_solver* s, uint64_t* last_step, uint64_t* total) {
+    int rc = check_handle(s, "rrsph_pair_count");
+    if (rc) return rc;
+    const int cur = (int)(s->step_index & 1);  // scalars the next step will use
+    rrsph::StepScalars h[2];
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(s->h_scal, s->scal + cur, sizeof(rrsph::StepScalars), cudaMemcpyDeviceToHost, s->stream));
+    RRSPH_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    h[0] = *s->h_scal;
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(s->h_scal, s->scal + (cur ^ 1), sizeof(rrsph::StepScalars), cudaMemcpyDeviceToHost, s->stream));
+    RRSPH_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    h[1] = *s->h_scal;
+    if (last_step) *last_step = s->step_index ? h[1].pairs : 0;
+    if (total) *total = h[0].pairs_total;
     return RRSPH_OK;
 }
 

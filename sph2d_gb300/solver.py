@@ -148,10 +148,27 @@ class Solver:
         check(lib().rrsph_step(self._h, nsteps, C.byref(t)))
         return t.value
 
+    def step_async(self, nsteps: int) -> None:
+        check(lib().rrsph_step_async(self._h, nsteps))
+
+    def set_time(self, time: float) -> None:
+        check(lib().rrsph_set_time(self._h, time))
+
+    def sync(self) -> float:
+        t = C.c_double()
+        check(lib().rrsph_sync(self._h, C.byref(t)))
+        return t.value
+
     def status(self, clear: bool = False) -> int:
         f = C.c_uint32()
         check(lib().rrsph_status(self._h, C.byref(f), 1 if clear else 0))
         return f.value
+
+    def pair_count(self):
+        """(pairs of the last step, pairs summed since upload)."""
+        a, b = C.c_uint64(), C.c_uint64()
+        check(lib().rrsph_pair_count(self._h, C.byref(a), C.byref(b)))
+        return int(a.value), int(b.value)
 
     def dt(self) -> float:
         d = C.c_double()

@@ -1,0 +1,429 @@
+"""Parity of the CUDA step (through the C ABI) with the reference.
+
+Bars (from the acceptance criteria of the step):
+- cell keys, sorted grid, cell starts and neighbour-pair sets: bit-exact;
+- FP64 step: density, pressure, accelerations and state after steps within
+  1e-5 relative L2 of the FP64 reference (asserted much tighter, 1e-10, since
+  the FP64 kernels follow the reference's summation order);
+- FP32-mixed step: same integer results; per-field errors against the FP64
+  oracle stated in the assertions below (density <= 1e-6, pressure <= 1e-4,
+  accelerations <= 1e-5 relative L2 after one evaluation).
+The reference results come from tests/golden/reference_fixtures.npz (the
+reference's own code, see tests/golden/make_golden.py) and from the C oracle.
+"""
+
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+sys.path.insert(0, str(GOLDEN))
+
+
+@pytest.fixture(scope="module")
+def fx():
+    return np.load(GOLDEN / "reference_fixtures.npz")
+
+
+def _flat(counts, lst):
+    return np.concatenate([lst[j, :counts[j]] for j in range(len(counts))]) if len(counts) else lst.ravel()[:0]
+
+
+# ------------------------------------------------- against the reference ---
+
+@pytest.mark.parametrize("name", ["dam", "flume"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_grid_and_pairs_bit_exact_vs_reference(gpu_available, fx, name, precision):
+    import make_golden as mg
+    from sph2d_gb300 import Solver
+
+    case = mg.fixture_cases()[name]
+    p = case.params()
+    with Solver(p, precision) as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        keys, grid, cs = s.grid_find()
+        counts, lst, tot = s.neighbours()
+    assert mg.digest(keys, grid, cs) == str(fx[f"{name}/grid_sha"])
+    assert mg.digest(counts, _flat(counts, lst)) == str(fx[f"{name}/pairs_sha"])
+    assert tot == int(fx[f"{name}/pairs"])
+
+
+@pytest.mark.parametrize("name", ["dam", "flume"])
+def test_fp64_density_forces_and_steps_vs_reference(gpu_available, fx, name):
+    import make_golden as mg
+    from sph2d_gb300 import Solver, capi
+
+    case = mg.fixture_cases()[name]
+    p = case.params()
+    with Solver(p, "fp64") as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        out, pres = s.density()
+    assert rel_l2(out, fx[f"{name}/density"]) < 1e-12
+    assert rel_l2(pres, fx[f"{name}/density_p"]) < 1e-12
+    v = mg.velocity_field(case)
+    q = p.copy()
+    q.dt_correction_method = 2
+    from oracle import binding as O
+
+    pr = O.eos_p(q, case.rho)
+    with Solver(q, "fp64") as s:
+        s.upload(case.r, v, case.rho, case.itype, pres=pr)
+        a, _, mu = s.forces(capi.TERM_ALL)
+    assert rel_l2(a, fx[f"{name}/terms_a"]) < 1e-12
+    assert rel_l2(mu, fx[f"{name}/terms_mu"]) < 1e-12
+    n = mg.RUN_STEPS[name]
+    with Solver(p, "fp64") as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        t = s.step(n, 0.0)
+        st = s.download()
+    for k in ("r", "v", "rho", "p"):
+        assert rel_l2(st[k], fx[f"{name}/run_{k}"]) < 1e-10, k
+    assert np.array_equal(st["itype"], fx[f"{name}/run_itype"])
+    assert t == pytest.approx(float(fx[f"{name}/run_time"]), rel=1e-13)
+
+
+# ---------------------------------------------- against the oracle (C) ---
+
+def _dam(**kw):
+    from sph2d_gb300 import cases
+
+    return cases.dam_break_2d(**kw)
+
+
+@pytest.mark.parametrize("treatment", [0, 1, 2])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_dam_break_full_size_vs_oracle(gpu_available, treatment, precision):
+    """The 2D dam break workload (5,000 fluid particles) one evaluation and 40 steps."""
+    from oracle import binding as O
+    from sph2d_gb300 import Solver, capi
+
+    case = _dam(density_treatment=min(treatment, 1))
+    p = case.params()
+    if treatment == 2:
+        p.density_treatment = 2
+        p.density_delta_sph_coef = 0.1
+    c_o, l_o, k_o, g_o, cs_o = O.neighbours(p, case.r, case.itype)
+    d_o, p_o = O.density(p, case.r, case.v, case.rho, case.itype)
+    with Solver(p, precision) as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        k, g, cs = s.grid_find()
+        c, lst, _ = s.neighbours()
+        d, pr = s.density()
+    assert np.array_equal(k, k_o) and np.array_equal(g, g_o) and np.array_equal(cs, cs_o)
+    assert np.array_equal(c, c_o) and np.array_equal(_flat(c, lst), _flat(c_o, l_o))
+    if precision == "fp64":
+        assert rel_l2(d, d_o) < 1e-12 and rel_l2(pr, p_o) < 1e-12
+    else:
+        assert rel_l2(d, d_o) < 1e-6, rel_l2(d, d_o)
+        assert rel_l2(pr, p_o) < 1e-4, rel_l2(pr, p_o)
+    ref = O.run(p, case.r, case.v, case.rho, case.itype, nsteps=40)
+    with Solver(p, precision) as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        t = s.step(40, 0.0)
+        st = s.download()
+    assert t == pytest.approx(ref["time"], rel=1e-13)
+    tol = {"fp64": dict(r=1e-12, v=1e-10, rho=1e-12, p=1e-9),
+           "mixed": dict(r=1e-8, v=1e-4, rho=1e-6, p=1e-3)}[precision]
+    for key, bound in tol.items():
+        assert rel_l2(st[key], ref[key]) < bound, (key, rel_l2(st[key], ref[key]))
+    assert np.array_equal(st["itype"], ref["itype"])
+
+
+SWITCHES = [
+    dict(),
+    dict(intf_sph_approximation=1),
+    dict(artificial_pressure=1),
+    dict(average_velocity=1, average_velocity_coef=0.05),
+    dict(boundary_treatment=0),
+    dict(artificial_bulk_visc=0.2),
+    dict(density_skf=3, intf_skf=3, artificial_viscosity_skf=3, average_velocity_skf=3, artificial_pressure_skf=3),
+    dict(density_skf=4, intf_skf=4, artificial_viscosity_skf=4, average_velocity_skf=4, artificial_pressure_skf=4),
+    dict(density_skf=2, intf_skf=2, artificial_viscosity_skf=2, average_velocity_skf=2, artificial_pressure_skf=2),
+]
+
+
+@pytest.mark.parametrize("sw", SWITCHES, ids=[",".join(f"{k}={v}" for k, v in s.items()) or "base" for s in SWITCHES])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_force_terms_switches_vs_oracle(gpu_available, sw, precision):
+    from oracle import binding as O
+    from sph2d_gb300 import Solver, capi, derive, params_from_json
+
+    case = _dam(nx=60, ny=30, seed=11)
+    model = dict(case.model)
+    model.update({k: v for k, v in sw.items()})
+    model["max_neighbours"] = 256  # the Gauss kernel's 3h cell sees more neighbours
+    p = derive(params_from_json(model, case.particle), case.r)
+    p.dt_correction_method = 2
+    rng = np.random.default_rng(5)
+    v = rng.normal(0, 0.3, size=case.r.shape)
+    pres = O.eos_p(p, case.rho) - 200.0
+    a_o, av_o, mu_o = O.forces(p, capi.TERM_ALL, case.r, v, case.rho, pres, case.itype)
+    with Solver(p, precision) as s:
+        s.upload(case.r, v, case.rho, case.itype, pres=pres)
+        a, av, mu = s.forces(capi.TERM_ALL, with_av=bool(p.average_velocity))
+    bound = 1e-12 if precision == "fp64" else 2e-5
+    assert rel_l2(a, a_o) < bound, rel_l2(a, a_o)
+    assert rel_l2(mu, mu_o) < (1e-12 if precision == "fp64" else 1e-5)
+    if p.average_velocity:
+        assert rel_l2(av, av_o) < (1e-12 if precision == "fp64" else 1e-5)
+
+
+@pytest.mark.parametrize("terms", [1, 2 | 1, 4, 8, 16])
+def test_single_terms_vs_oracle(gpu_available, terms):
+    from oracle import binding as O
+    from sph2d_gb300 import Solver
+
+    case = _dam(nx=40, ny=20, seed=3)
+    p = case.params()
+    p.average_velocity = 1
+    p.average_velocity_coef = 0.05
+    rng = np.random.default_rng(9)
+    v = rng.normal(0, 0.2, size=case.r.shape)
+    pres = O.eos_p(p, case.rho)
+    a_o, av_o, _ = O.forces(p, terms, case.r, v, case.rho, pres, case.itype)
+    with Solver(p, "fp64") as s:
+        s.upload(case.r, v, case.rho, case.itype, pres=pres)
+        a, av, _ = s.forces(terms, with_av=True)
+    assert rel_l2(a, a_o) < 1e-12
+    assert rel_l2(av, av_o) < 1e-12
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_dam_break_3d_vs_oracle(gpu_available, precision):
+    from oracle import binding as O
+    from sph2d_gb300 import Solver, cases
+
+    case = cases.dam_break_3d(dx=0.02, tank=(0.5, 0.2, 0.3), block=(0.2, 0.2, 0.15), max_neighbours=400)
+    p = case.params()
+    c_o, l_o, k_o, g_o, cs_o = O.neighbours(p, case.r, case.itype)
+    ref = O.run(p, case.r, case.v, case.rho, case.itype, nsteps=10)
+    with Solver(p, precision) as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        k, g, cs = s.grid_find()
+        c, lst, _ = s.neighbours()
+        s.upload(case.r, case.v, case.rho, case.itype)
+        t = s.step(10, 0.0)
+        st = s.download()
+    assert np.array_equal(k, k_o) and np.array_equal(g, g_o) and np.array_equal(cs, cs_o)
+    assert np.array_equal(c, c_o) and np.array_equal(_flat(c, lst), _flat(c_o, l_o))
+    tol = dict(r=1e-12, v=1e-9, rho=1e-12) if precision == "fp64" else dict(r=1e-8, v=1e-4, rho=1e-6)
+    for key, bound in tol.items():
+        assert rel_l2(st[key], ref[key]) < bound, (key, rel_l2(st[key], ref[key]))
+
+
+def test_flume_full_size_fp64_one_step_vs_oracle(gpu_available):
+    """The 2D piston flume workload at full size (about 409k particles)."""
+    from oracle import binding as O
+    from sph2d_gb300 import Solver, cases
+
+    case = cases.piston_flume_2d()
+    p = case.params()
+    ref = O.run(p, case.r, case.v, case.rho, case.itype, nsteps=2)
+    with Solver(p, "fp64") as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        t = s.step(2, 0.0)
+        st = s.download()
+    for key in ("r", "v", "rho", "p"):
+        assert rel_l2(st[key], ref[key]) < 1e-10, key
+    with Solver(p, "mixed") as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        s.step(2, 0.0)
+        sm = s.download()
+    assert rel_l2(sm["rho"], ref["rho"]) < 1e-6
+    assert rel_l2(sm["v"], ref["v"]) < 1e-4
+
+
+# ------------------------------------------------------------ edge cases ---
+
+def test_wave_makers_vs_oracle(gpu_available):
+    """Piston 2nd order, wall disappear and solitary-wave piston."""
+    from oracle import binding as O
+    from sph2d_gb300 import Solver, cases
+
+    for nwm, extra in ((3, {}), (4, {"nwm_time_start": 0.0005}), (5, {"nwm_wave_magnitude": 0.05})):
+        case = cases.piston_flume_2d(nx=150, ny=20)
+        p = case.params()
+        p.nwm = nwm
+        for k, v in extra.items():
+            setattr(p, k, v)
+        ref = O.run(p, case.r, case.v, case.rho, case.itype, nsteps=25)
+        with Solver(p, "fp64") as s:
+            s.upload(case.r, case.v, case.rho, case.itype)
+            s.step(25, 0.0)
+            st = s.download()
+        for key in ("r", "v", "rho"):
+            assert rel_l2(st[key], ref[key]) < 1e-10, (nwm, key)
+        assert np.array_equal(st["itype"], ref["itype"]), nwm
+
+
+def test_non_existent_particles_are_skipped(gpu_available):
+    from oracle import binding as O
+    from sph2d_gb300 import Solver
+
+    case = _dam(nx=40, ny=20)
+    itype = case.itype.copy()
+    itype[::7] = 0
+    p = case.params()
+    c_o, l_o, *_ = O.neighbours(p, case.r, itype)
+    ref = O.run(p, case.r, case.v, case.rho, itype, nsteps=5)
+    with Solver(p, "fp64") as s:
+        s.upload(case.r, case.v, case.rho, itype)
+        c, lst, _ = s.neighbours()
+        s.upload(case.r, case.v, case.rho, itype)
+        s.step(5, 0.0)
+        st = s.download()
+    assert np.array_equal(c, c_o) and np.array_equal(_flat(c, lst), _flat(c_o, l_o))
+    assert rel_l2(st["v"], ref["v"]) < 1e-10
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 2047, 2049])
+def test_ragged_and_tiny_particle_counts(gpu_available, n):
+    """Counts that are not a multiple of any tile size, including one particle."""
+    from oracle import binding as O
+    from sph2d_gb300 import Solver
+
+    base = _dam(nx=60, ny=40)
+    idx = np.random.default_rng(n).choice(base.ntotal, size=n, replace=False)
+    idx.sort()
+    particle = dict(base.particle, ntotal=n, nfluid=int(np.sum(idx < base.particle["nfluid"])),
+                    nvirt=int(np.sum(idx >= base.particle["nfluid"])))
+    from sph2d_gb300 import derive, params_from_json
+
+    r, v, rho, it = base.r[idx], base.v[idx], base.rho[idx], base.itype[idx]
+    p = derive(params_from_json(base.model, particle), r)
+    c_o, l_o, k_o, g_o, cs_o = O.neighbours(p, r, it)
+    ref = O.run(p, r, v, rho, it, nsteps=3)
+    with Solver(p, "fp64") as s:
+        s.upload(r, v, rho, it)
+        k, g, cs = s.grid_find()
+        c, lst, _ = s.neighbours()
+        s.upload(r, v, rho, it)
+        s.step(3, 0.0)
+        st = s.download()
+    assert np.array_equal(k, k_o) and np.array_equal(g, g_o) and np.array_equal(cs, cs_o)
+    assert np.array_equal(c, c_o) and np.array_equal(_flat(c, lst), _flat(c_o, l_o))
+    assert rel_l2(st["r"], ref["r"]) < 1e-12
+
+
+def test_out_of_domain_is_an_error(gpu_available):
+    from sph2d_gb300 import RrsphError, Solver, capi
+
+    case = _dam(nx=20, ny=10)
+    p = case.params()
+    r = case.r.copy()
+    r[3] = [p.x_maxgeom + 50.0, 0.5]  # far outside: Morton key >= max_cells
+    with Solver(p, "fp64") as s:
+        s.upload(r, case.v, case.rho, case.itype)
+        with pytest.raises(RrsphError) as e:
+            s.step(1, 0.0)
+        assert e.value.code == capi.ERR_OUT_OF_DOMAIN
+        assert s.status() & capi.FLAG_OUT_OF_DOMAIN
+
+
+def test_neighbour_overflow_is_an_error(gpu_available):
+    from oracle import binding as O
+    from sph2d_gb300 import RrsphError, Solver, capi
+
+    case = _dam(nx=20, ny=10)
+    p = case.params()
+    p.max_neighbours = 8
+    with pytest.raises(O.OracleError):
+        O.neighbours(p, case.r, case.itype)
+    with Solver(p, "fp64") as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        with pytest.raises(RrsphError) as e:
+            s.step(1, 0.0)
+        assert e.value.code == capi.ERR_NEIGHBOUR_OVERFLOW
+        with pytest.raises(RrsphError):
+            s.density()
+
+
+def test_consistency_stop_and_fix(gpu_available):
+    from oracle import binding as O
+    from sph2d_gb300 import RrsphError, Solver, capi
+
+    case = _dam(nx=20, ny=10)
+    p = case.params()
+    v = case.v.copy()
+    v[0] = [0.0, -1.0e4]  # leaves the geometry box in one step
+    q = p.copy()
+    q.consistency_treatment = 1
+    with Solver(q, "fp64") as s:
+        s.upload(case.r, v, case.rho, case.itype)
+        with pytest.raises(RrsphError) as e:
+            s.step(1, 0.0)
+        assert e.value.code == capi.ERR_OUTSIDE_GEOMETRY
+    q.consistency_treatment = 2  # CONSISTENCY_FIX: the particle becomes non-existent
+    ref = O.run(q, case.r, v, case.rho, case.itype, nsteps=2)
+    with Solver(q, "fp64") as s:
+        s.upload(case.r, v, case.rho, case.itype)
+        s.step(2, 0.0)
+        st = s.download()
+    assert st["itype"][0] == 0 and np.array_equal(st["itype"], ref["itype"])
+    assert rel_l2(st["r"], ref["r"]) < 1e-12
+
+
+def test_dynamic_dt_follows_the_omp_build(gpu_available):
+    """DT_CORRECTION_DYNAMIC: the OpenMP build's reduction is compiled out, so
+    every step uses dt = CFL*h/c (UpdateAcceleration.cpp:107-124)."""
+    from oracle import binding as O
+    from sph2d_gb300 import Solver
+
+    case = _dam(nx=30, ny=15)
+    p = case.params()
+    p.dt_correction_method = 2
+    p.CFL_coef = 0.2
+    p.dt = 0.0
+    with Solver(p, "fp64") as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        t = s.step(5, 0.0)
+        dt = s.dt()
+    c = float(np.sqrt(O.lib().orc_eos_c_sqr(__import__("ctypes").byref(p))))
+    assert dt == pytest.approx(0.2 * p.hsml / c, rel=1e-14)
+    assert t == pytest.approx(5 * dt, rel=1e-12)
+
+
+def test_graph_replay_equals_direct_launches(gpu_available):
+    from sph2d_gb300 import Solver
+
+    case = _dam(nx=50, ny=25)
+    p = case.params()
+    out = []
+    for timing in (False, True):
+        with Solver(p, "fp64") as s:
+            s.set_phase_timing(timing)
+            s.upload(case.r, case.v, case.rho, case.itype)
+            s.step(7, 0.0)
+            out.append(s.download())
+            if timing:
+                times, steps = s.phase_times()
+                assert steps == 7 and all(v > 0 for v in times.values())
+            assert s.kernel_launches() > 0
+    for k in ("r", "v", "rho", "p"):
+        assert np.array_equal(out[0][k], out[1][k]), k
+
+
+def test_stepping_in_chunks_equals_one_call(gpu_available):
+    from sph2d_gb300 import Solver
+
+    case = _dam(nx=50, ny=25)
+    p = case.params()
+    with Solver(p, "fp64") as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        t = s.step(9, 0.0)
+        a = s.download()
+    with Solver(p, "fp64") as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        t2 = 0.0
+        for n in (1, 3, 5):
+            t2 = s.step(n, t2)
+        b = s.download()
+    assert t == t2
+    for k in ("r", "v", "rho", "p"):
+        assert np.array_equal(a[k], b[k]), k
