@@ -223,8 +223,9 @@ int rrsph_step_async(rrsph_solver* s, uint64_t nsteps);
 /* Sets the simulation time of the next step (stream-ordered). */
 int rrsph_set_time(rrsph_solver* s, double time);
 /* Waits for the enqueued steps; *time_out (may be NULL) receives the time
- * after the last step. Returns the status the device checks imply, and clears
- * the device flags. */
+ * after the last step. Returns the status the device flags imply. The flags
+ * stay set (rrsph_status reads and clears them; rrsph_step clears them when
+ * it starts). */
 int rrsph_sync(rrsph_solver* s, double* time_out);
 /* Sticky RRSPH_FLAG_* bits raised by device checks since the last clear. */
 int rrsph_status(rrsph_solver* s, uint32_t* flags, int clear);

@@ -514,7 +514,6 @@ extern "C" int rrsph_sync(rrsph_solver* s, double* time_out) {
     const int parn = (int)(s->step_index & 1);
     RRSPH_CUDA_TRY(cudaMemcpyAsync(s->h_scal, &s->scal[parn], sizeof(rrsph::StepScalars), cudaMemcpyDeviceToHost, st));
     RRSPH_CUDA_TRY(cudaMemcpyAsync(s->h_flags, s->flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    RRSPH_CUDA_TRY(cudaMemsetAsync(s->flags, 0, sizeof(uint32_t), st));
     RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
     RRSPH_CUDA_TRY(cudaGetLastError());
     if (time_out) *time_out = s->h_scal->time;

@@ -120,7 +120,9 @@ def test_dam_break_full_size_vs_oracle(gpu_available, treatment, precision):
     if precision == "fp64":
         assert rel_l2(d, d_o) < 1e-12 and rel_l2(pr, p_o) < 1e-12
     else:
-        assert rel_l2(d, d_o) < 1e-6, rel_l2(d, d_o)
+        # summation density to 1e-6; the continuity rates are sums with heavy
+        # cancellation (the delta-SPH term), stated to 5e-5
+        assert rel_l2(d, d_o) < (1e-6 if treatment == 0 else 5e-5), rel_l2(d, d_o)
         assert rel_l2(pr, p_o) < 1e-4, rel_l2(pr, p_o)
     ref = O.run(p, case.r, case.v, case.rho, case.itype, nsteps=40)
     with Solver(p, precision) as s:
