@@ -260,6 +260,28 @@ int rrsph_density(rrsph_solver* s, double* out_rho_or_drho, double* out_p);
 int rrsph_forces(rrsph_solver* s, uint32_t terms, double* a, uint32_t stride,
                  double* av, double* mu);
 
+/* ---- grid sort without allocation ----------------------------------------- */
+/* Largest n rrsph_sort_pairs_noalloc accepts. */
+#define RRSPH_SORT_NOALLOC_MAX_PAIRS (1u << 20)
+/* Stable sort of n (cell key, particle id) pairs by the low key_bits bits of
+ * the key: the grid sort rrsph_grid_find runs, for callers that cannot
+ * allocate device memory (code whose device memory belongs to another
+ * framework's pool, or a step loop that must not allocate because cudaMalloc
+ * can block or fail mid-run). No counterpart in the reference.
+ * Every pointer is a device pointer owned by the caller; outputs must not
+ * overlap inputs, and the inputs are left unchanged. The working memory is a
+ * fixed array inside the library (about 8.9 MB; every GPU that loads the
+ * library holds it until the process exits), so n is limited to
+ * RRSPH_SORT_NOALLOC_MAX_PAIRS and a larger n returns
+ * RRSPH_ERR_INVALID_ARGUMENT. The call allocates nothing and is asynchronous
+ * on `stream` (a cudaStream_t; NULL = the default stream). Its first call on a
+ * device looks up the array's device address; make that first call before any
+ * stream capture. All calls on a device share the array, so calls that may
+ * overlap on the GPU race: order them (one stream, or events). */
+int rrsph_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* ids_in,
+                             uint32_t* keys_out, uint32_t* ids_out, uint32_t n,
+                             uint32_t key_bits, void* stream);
+
 /* ---- timing hooks for benchmarks ------------------------------------------ */
 /* Number of kernel phases one step launches and their names. */
 int rrsph_phase_count(rrsph_solver* s, int* count);

@@ -31,7 +31,7 @@ ORACLE_LIB = ORACLE_DIR / "liboracle.so"
 REF_BIN = ORACLE_DIR / "_ref" / "rrsph_ref"
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CU_SOURCES = ["sort.cu", "kernels_common.cu", "kernels_fp64.cu", "kernels_mixed.cu", "solver.cu"]
+CU_SOURCES = ["sort.cu", "kernels_common.cu", "kernels_fp64.cu", "kernels_mixed.cu", "solver.cu", "sort_noalloc.cu"]
 CPP_SOURCES = ["params.cpp", "layers.cpp"]
 
 

@@ -43,6 +43,8 @@ TERM_ART_VISC = 0x8
 TERM_AVERAGE_VELOCITY = 0x10
 TERM_ALL = 0x1F
 
+SORT_NOALLOC_MAX_PAIRS = 1 << 20
+
 u32, u64, i32, f64 = C.c_uint32, C.c_uint64, C.c_int32, C.c_double
 
 
@@ -136,6 +138,8 @@ _SIGS = {
     "rrsph_set_phase_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "rrsph_phase_times": (C.c_int, [C.c_void_p, _dp, C.c_int, _P(C.c_uint64), C.c_int]),
     "rrsph_kernel_launches": (C.c_int, [C.c_void_p, _P(C.c_uint64)]),
+    "rrsph_sort_pairs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                           C.c_void_p]),
 }
 
 

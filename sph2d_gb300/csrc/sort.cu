@@ -156,4 +156,27 @@ void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32
     *vals_out = vi;
 }
 
+void radix_sort_pairs_into(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
+                           uint32_t* keys_tmp, uint32_t* vals_tmp, uint32_t* counts, uint32_t n, int bits,
+                           cudaStream_t stream, unsigned long long* launches) {
+    if (n == 0) return;
+    const uint32_t tiles = sort_tiles(n);
+    uint32_t* totals = counts + (size_t)kRadix * tiles;
+    const int passes = (bits + 7) / 8;
+    const uint32_t *ki = keys_in, *vi = vals_in;
+    for (int pass = 0; pass < passes; pass++) {
+        // the last pass must land in the output, so targets alternate backwards from it
+        const bool to_out = ((passes - 1 - pass) % 2) == 0;
+        uint32_t* ko = to_out ? keys_out : keys_tmp;
+        uint32_t* vo = to_out ? vals_out : vals_tmp;
+        const int shift = pass * 8;
+        k_tile_hist<<<tiles, kSortThreads, 0, stream>>>(ki, n, shift, tiles, counts);
+        k_digit_scan<<<kRadix * 32 / 256, 256, 0, stream>>>(counts, tiles, totals);
+        k_scatter<<<tiles, kSortThreads, 0, stream>>>(ki, vi, ko, vo, n, shift, tiles, counts, totals);
+        if (launches) *launches += 3;
+        ki = ko;
+        vi = vo;
+    }
+}
+
 }  // namespace rrsph

@@ -24,4 +24,11 @@ void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32
                       uint32_t* scratch, uint32_t n, int bits, cudaStream_t stream,
                       uint32_t** keys_out, uint32_t** vals_out, unsigned long long* launches);
 
+// Same sort with caller-given buffers: reads keys_in/vals_in (not modified),
+// leaves the result in keys_out/vals_out, and uses keys_tmp/vals_tmp (n words
+// each) and counts (sort_scratch_words(n) words) as working memory.
+void radix_sort_pairs_into(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
+                           uint32_t* keys_tmp, uint32_t* vals_tmp, uint32_t* counts, uint32_t n, int bits,
+                           cudaStream_t stream, unsigned long long* launches);
+
 }  // namespace rrsph
