@@ -42,8 +42,9 @@ L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
 
 # Algorithmic bytes per particle of the dominant kernel (the force gather) of
 # the FP32-mixed 2D step: reads cell key 4, id 4, position+type float4 16,
-# velocity+density float4 16, pressure 4; writes a.x, a.y as double 16.
-FORCES_MIXED_BYTES_PER_PARTICLE = 60
+# velocity+density float4 16, (p, p/rho^2) float2 8, the 10 neighbour-mask words
+# the density pass wrote 40; writes a.x, a.y as double 16.
+FORCES_MIXED_BYTES_PER_PARTICLE = 100
 FORCES_FP64_BYTES_PER_PARTICLE_2D = 4 + 4 + 16 + 4 + 16 + 8 + 8 + 16
 
 

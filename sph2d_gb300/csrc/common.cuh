@@ -18,6 +18,8 @@ struct MixedF {
     float cut2_lo, cut2_hi;     // guard band around the cutoff: pairs inside it are re-tested in double
     float kf[5];                // kernel factors by skf
     float w0_density;           // mass * W(0)
+    float rho0_minus_w0_hi, rho0_minus_w0_lo;  // rho0 - mass*W(0) as an unevaluated float sum
+    float B, inv_rho0;          // EOS constants
     float lj_rr0, lj_D, etq_h2;
     float av_alpha_c, av_beta;  // alpha * c, beta
     float ap_coef, ap_index, ap_inv_wdelta;
@@ -126,6 +128,20 @@ __device__ inline uint64_t cell_coord(double r, double rmin, double cell) {
     if (!(c >= 0.0)) return 0;
     if (c >= 18446744073709551615.0) return ~0ull;
     return (uint64_t)c;
+}
+
+// The same truncation with a multiply by 1/cell instead of the division. The
+// product is within 2 ulp of the correctly rounded quotient, so the two
+// truncate alike unless the quotient lies within 1e-9 of an integer; there the
+// exact division decides.
+__device__ inline uint64_t cell_coord_fast(double r, double rmin, double cell, double inv_cell) {
+    const double d = __dsub_rn(r, rmin);
+    const double q = __dmul_rn(d, inv_cell);
+    if (!(q >= 0.0) || !(q < 4.0e9)) return cell_coord(r, rmin, cell);
+    const double t = trunc(q);
+    const double frac = q - t;
+    if (frac > 1e-9 && frac < 1.0 - 1e-9) return (uint64_t)t;
+    return cell_coord(r, rmin, cell);
 }
 
 // Neighbour-cell coordinate steps (GridUtils.h:158-163).

@@ -41,6 +41,11 @@ struct Sorted {
     float4* V4;    // velocity the forces use + density the forces use
     float4* VD4;   // v + (rho - rho0) for density_con
     float2* PR;    // pressure p and p / rho^2 (rho = the density the forces use)
+    // 2D mixed step: neighbour masks written by the density pass for the force
+    // pass, SoA [10][n]: word c < 9 = bit b set if particle cell_start + b of
+    // stencil cell c is a neighbour; word 9 = stencil cells with more than 32
+    // particles (searched again by the force pass). Null where unused.
+    uint32_t* nbmask;
 };
 
 // Sources the reorder gathers for the force velocity / density.
@@ -66,10 +71,11 @@ void launch_density_mixed(const DevParams& P, const State& S, const Sorted& G, S
                           cudaStream_t st);
 template <int DIM>
 void launch_forces_mixed(const DevParams& P, const State& S, const Sorted& G, uint32_t terms, StepScalars* scal,
-                         uint32_t* flags, int write_mu, cudaStream_t st);
+                         uint32_t* flags, int write_mu, int use_masks, cudaStream_t st);
+// whole_step; with next_keys also the next step's predict_half_step and key pass.
 template <int DIM>
-void launch_whole_step(const DevParams& P, const State& S, StepScalars* scal_cur, StepScalars* scal_next,
-                       uint32_t* flags, cudaStream_t st);
+void launch_whole_step(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal_cur,
+                       StepScalars* scal_next, uint32_t* flags, int next_keys, cudaStream_t st);
 
 void launch_cells_start(const DevParams& P, const Sorted& G, uint32_t* out, cudaStream_t st);
 template <int DIM>

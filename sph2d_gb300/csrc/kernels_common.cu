@@ -14,27 +14,18 @@ inline unsigned blocks_for(uint32_t n, int threads) { return (n + threads - 1) /
 // key pass of make_grid (RRSPH_OMP/src/GridFind.cpp:55-75). Also clears the
 // cell-table entries of the previous grid (key_of) so that the table needs no
 // max_cells-sized reset.
+// Cell key of particle i at (x, y, z) (GridFind.cpp:55-75); also clears the
+// previous grid's cell-table entry of i and records the new key.
 template <int DIM>
-__global__ void k_keys(DevParams P, State S, Sorted G, const StepScalars* __restrict__ scal, int predict,
-                       uint32_t* __restrict__ flags) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    if (predict) {
-        const double dt = scal->dt;
-        S.vpx[i] = S.vx[i] + S.ax[i] * dt * 0.5;
-        S.vpy[i] = S.vy[i] + S.ay[i] * dt * 0.5;
-        if (DIM == 3) S.vpz[i] = S.vz[i] + S.az[i] * dt * 0.5;
-        if (P.density_treatment != 0) S.rho_pred[i] = S.rho[i] + S.drho[i] * dt * 0.5;
-    }
-    const double x = S.rx[i], y = S.ry[i];
+__device__ __forceinline__ void key_pass(const DevParams& P, const State& S, const Sorted& G, uint32_t i, double x,
+                                         double y, double z, uint32_t* __restrict__ flags) {
     bool outside = !(x >= P.xmin) || !(y >= P.ymin);
-    const uint64_t cx = cell_coord(x, P.xmin, P.cell);
-    const uint64_t cy = cell_coord(y, P.ymin, P.cell);
+    const uint64_t cx = cell_coord_fast(x, P.xmin, P.cell, P.inv_cell);
+    const uint64_t cy = cell_coord_fast(y, P.ymin, P.cell, P.inv_cell);
     uint64_t key;
     if (DIM == 3) {
-        const double z = S.rz[i];
         outside = outside || !(z >= P.zmin);
-        const uint64_t cz = cell_coord(z, P.zmin, P.cell);
+        const uint64_t cz = cell_coord_fast(z, P.zmin, P.cell, P.inv_cell);
         key = split3(cx) | (split3(cy) << 1) | (split3(cz) << 2);
     } else {
         key = split2(cx) | (split2(cy) << 1);
@@ -49,6 +40,27 @@ __global__ void k_keys(DevParams P, State S, Sorted G, const StepScalars* __rest
     S.key_of[i] = (uint32_t)key;
     G.keys_in[i] = (uint32_t)key;
     G.ids_in[i] = i;
+}
+
+// predict_half_step (PredictHalfStep.cpp:4-23) of particle i with time step dt.
+template <int DIM>
+__device__ __forceinline__ void predict(const DevParams& P, const State& S, uint32_t i, double vx, double vy,
+                                        double vz, double rho, double dt) {
+    S.vpx[i] = vx + S.ax[i] * dt * 0.5;
+    S.vpy[i] = vy + S.ay[i] * dt * 0.5;
+    if (DIM == 3) S.vpz[i] = vz + S.az[i] * dt * 0.5;
+    if (P.density_treatment != 0) S.rho_pred[i] = rho + S.drho[i] * dt * 0.5;
+}
+
+template <int DIM>
+__global__ void k_keys(DevParams P, State S, Sorted G, const StepScalars* __restrict__ scal, int do_predict,
+                       uint32_t* __restrict__ flags) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    if (do_predict)
+        predict<DIM>(P, S, i, S.vx[i], S.vy[i], DIM == 3 ? S.vz[i] : 0.0, P.density_treatment ? S.rho[i] : 0.0,
+                     scal->dt);
+    key_pass<DIM>(P, S, G, i, S.rx[i], S.ry[i], DIM == 3 ? S.rz[i] : 0.0, flags);
 }
 
 // Gathers the state into cell order and records each cell's [start, end) in
@@ -135,8 +147,8 @@ __device__ double solitary_vx(const DevParams& P, double time) {
 // RRSPHOutput::update_step (RRSPH_COMMON/src/Output.cpp:395-416). Thread 0
 // advances the step scalars into scal_next (time += dt, step + 1).
 template <int DIM>
-__global__ void k_whole(DevParams P, State S, const StepScalars* __restrict__ scal, StepScalars* __restrict__ next,
-                        uint32_t* __restrict__ flags) {
+__global__ void k_whole(DevParams P, State S, Sorted G, const StepScalars* __restrict__ scal,
+                        StepScalars* __restrict__ next, uint32_t* __restrict__ flags, int next_keys) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     // update_dt (UpdateAcceleration.cpp:15-29) under DT_CORRECTION_DYNAMIC
     double dt = scal->dt;
@@ -172,12 +184,17 @@ __global__ void k_whole(DevParams P, State S, const StepScalars* __restrict__ sc
         }
     }
     const double v_dt = scal->step ? dt : dt * 0.5;
-    if (P.density_treatment != 0) S.rho[i] = S.rho[i] + S.drho[i] * v_dt;
+    double rho = 0.0;
+    if (P.density_treatment != 0) {
+        rho = S.rho[i] + S.drho[i] * v_dt;
+        S.rho[i] = rho;
+    }
     double x = S.rx[i], y = S.ry[i], z = DIM == 3 ? S.rz[i] : 0.0;
+    double vx = S.vx[i], vy = S.vy[i], vz = DIM == 3 ? S.vz[i] : 0.0;
     if (S.itype[i] > 0) {
-        double vx = S.vx[i] + S.ax[i] * v_dt;
-        double vy = S.vy[i] + S.ay[i] * v_dt;
-        double vz = DIM == 3 ? S.vz[i] + S.az[i] * v_dt : 0.0;
+        vx = vx + S.ax[i] * v_dt;
+        vy = vy + S.ay[i] * v_dt;
+        if (DIM == 3) vz = vz + S.az[i] * v_dt;
         if (P.avg_vel) {
             vx += S.avx[i];
             vy += S.avy[i];
@@ -207,6 +224,11 @@ __global__ void k_whole(DevParams P, State S, const StepScalars* __restrict__ sc
         bool in = x < P.xmax && x > P.xmin && y < P.ymax && y > P.ymin;
         if (DIM == 3) in = in && z < P.zmax && z > P.zmin;
         if (!in) atomicOr(flags, RRSPH_FLAG_OUTSIDE_GEOMETRY);
+    }
+    if (next_keys) {
+        // the next step's predict_half_step and cell keys, from the state just written
+        predict<DIM>(P, S, i, vx, vy, vz, rho, dt);
+        key_pass<DIM>(P, S, G, i, x, y, z, flags);
     }
 }
 
@@ -300,9 +322,9 @@ void launch_reorder(const DevParams& P, const State& S, const Sorted& G, GatherS
     k_reorder<DIM><<<blocks_for(P.n, 256), 256, 0, st>>>(P, S, G, fsrc, mixed);
 }
 template <int DIM>
-void launch_whole_step(const DevParams& P, const State& S, StepScalars* scal_cur, StepScalars* scal_next,
-                       uint32_t* flags, cudaStream_t st) {
-    k_whole<DIM><<<blocks_for(P.n, 256), 256, 0, st>>>(P, S, scal_cur, scal_next, flags);
+void launch_whole_step(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal_cur,
+                       StepScalars* scal_next, uint32_t* flags, int next_keys, cudaStream_t st) {
+    k_whole<DIM><<<blocks_for(P.n, 256), 256, 0, st>>>(P, S, G, scal_cur, scal_next, flags, next_keys);
 }
 void launch_cells_start(const DevParams& P, const Sorted& G, uint32_t* out, cudaStream_t st) {
     const uint64_t m = (uint64_t)P.max_cells + 1;
@@ -326,8 +348,8 @@ void launch_pack(const DevParams& P, State S, double* r, double* v, uint32_t str
     template void launch_keys<D>(const DevParams&, const State&, Sorted&, StepScalars*, int, uint32_t*,        \
                                  cudaStream_t);                                                                \
     template void launch_reorder<D>(const DevParams&, const State&, const Sorted&, GatherSrc, int, cudaStream_t); \
-    template void launch_whole_step<D>(const DevParams&, const State&, StepScalars*, StepScalars*, uint32_t*,  \
-                                       cudaStream_t);                                                          \
+    template void launch_whole_step<D>(const DevParams&, const State&, const Sorted&, StepScalars*,            \
+                                       StepScalars*, uint32_t*, int, cudaStream_t);                            \
     template void launch_neighbour_list<D>(const DevParams&, const Sorted&, uint32_t*, uint32_t*, uint32_t,    \
                                            uint32_t*, cudaStream_t);                                           \
     template void launch_unpack<D>(const DevParams&, State, const double*, const double*, uint32_t, cudaStream_t); \

@@ -46,14 +46,13 @@ __global__ void __launch_bounds__(kGatherThreads) k_density(DevParams P, State S
         const double f = P.kf[skf];
         double acc = cont ? 0.0 : P.mass * P.w0_density;
         if (G.itype[k] != P.type_non_existent) {
-            uint64_t cx, cy, cz;
-            decode_key<DIM>(G.key[k], cx, cy, cz);
+            const Stencil<DIM> st(P, G.key[k]);
             constexpr int NC = DIM == 3 ? 27 : 9;
 #pragma unroll 1
             for (int c = 0; c < NC; c++) {
                 uint32_t cell;
                 int sx, sy, sz;
-                if (!stencil_cell<DIM>(P, cx, cy, cz, c, cell, sx, sy, sz)) continue;
+                if (!st.cell(c, cell, sx, sy, sz)) continue;
                 const uint32_t s = G.cell_start[cell];
                 if (s == kEmpty) continue;
                 const uint32_t e = G.cell_end[cell];
@@ -130,14 +129,13 @@ __global__ void __launch_bounds__(kGatherThreads) k_forces(DevParams P, State S,
         const bool avel = (terms & RRSPH_TERM_AVERAGE_VELOCITY) && P.avg_vel;
         const double pj_r2 = pj / (rhoj * rhoj);
         if (tj != P.type_non_existent) {
-            uint64_t cx, cy, cz;
-            decode_key<DIM>(G.key[k], cx, cy, cz);
+            const Stencil<DIM> st(P, G.key[k]);
             constexpr int NC = DIM == 3 ? 27 : 9;
 #pragma unroll 1
             for (int c = 0; c < NC; c++) {
                 uint32_t cell;
                 int sx, sy, sz;
-                if (!stencil_cell<DIM>(P, cx, cy, cz, c, cell, sx, sy, sz)) continue;
+                if (!st.cell(c, cell, sx, sy, sz)) continue;
                 const uint32_t s = G.cell_start[cell];
                 if (s == kEmpty) continue;
                 const uint32_t e = G.cell_end[cell];

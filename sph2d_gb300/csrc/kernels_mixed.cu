@@ -95,6 +95,16 @@ __device__ __forceinline__ void warp_max_bits(unsigned long long* dst, double v)
     if ((threadIdx.x & 31) == 0 && v > 0) atomicMax(dst, dbits(v));
 }
 
+// eos_art_p (EOS.cpp:31-34) in float on the density deviation d = rho - rho0:
+// (rho/rho0)^7 - 1 = t (1 + x + ... + x^6) with t = d/rho0, x = 1 + t, which
+// has no cancellation, so p keeps float accuracy relative to itself.
+__device__ __forceinline__ float eos_pf(const MixedF& M, float d) {
+    const float t = d * M.inv_rho0;
+    const float x = 1.0f + t;
+    const float sum = 1.0f + x * (1.0f + x * (1.0f + x * (1.0f + x * (1.0f + x * (1.0f + x)))));
+    return M.B * t * sum;
+}
+
 // density_sum / density_con (Density.h:25-114) + EOS. SKF: 1 = cubic only
 // (every kernel choice cubic), 0 = any kernel (runtime switch).
 template <int DIM, int SKF>
@@ -116,22 +126,28 @@ __global__ void __launch_bounds__(kGatherThreads) k_density_mixed(DevParams P, S
         const int skf = SKF ? SKF : P.density_skf;
         const float f = M.kf[skf];
         Kahan acc{0.0f, 0.0f};
+        const bool masks = DIM == 2 && G.nbmask != nullptr;
+        uint32_t over = 0;
+        // 2D: the neighbour masks of the 9 cells, kept in registers and stored
+        // together at the end so the stores stay coalesced
+        uint32_t m0 = 0, m1 = 0, m2 = 0, m3 = 0, m4 = 0, m5 = 0, m6 = 0, m7 = 0, m8 = 0;
+        constexpr int NC = DIM == 3 ? 27 : 9;
         if (tj != P.type_non_existent) {
-            uint64_t cx, cy, cz;
-            decode_key<DIM>(G.key[k], cx, cy, cz);
-            constexpr int NC = DIM == 3 ? 27 : 9;
+            const Stencil<DIM> st(P, G.key[k]);
 #pragma unroll 1
             for (int c = 0; c < NC; c++) {
                 uint32_t cell;
                 int sx, sy, sz;
-                if (!stencil_cell<DIM>(P, cx, cy, cz, c, cell, sx, sy, sz)) continue;
+                if (!st.cell(c, cell, sx, sy, sz)) continue;
                 const uint32_t s = G.cell_start[cell];
                 if (s == kEmpty) continue;
                 const uint32_t e = G.cell_end[cell];
+                if (e - s > 32) over |= 1u << c;
                 const float shx = (float)sx * M.cell - pj.x;
                 const float shy = (float)sy * M.cell - pj.y;
                 const float shz = DIM == 3 ? (float)sz * M.cell - pj.z : 0.0f;
                 float part = 0.0f;
+                uint32_t bits = 0;
                 for (uint32_t i = s; i < e; i++) {
                     if (i == k) continue;
                     const float4 pi = G.P4[i];
@@ -140,6 +156,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_density_mixed(DevParams P, S
                     const float d2 = DIM == 3 ? dx * dx + dy * dy + dz * dz : dx * dx + dy * dy;
                     if (!within_cutoff<DIM>(P, G, i, k, d2)) continue;
                     cnt++;
+                    if (i - s < 32) bits |= 1u << (i - s);
                     const float inv_dist = rsqrtf(d2);
                     const float q = d2 * inv_dist * M.inv_h;
                     if (!cont) {
@@ -159,21 +176,51 @@ __global__ void __launch_bounds__(kGatherThreads) k_density_mixed(DevParams P, S
                         part += term;
                     }
                 }
+                if (masks) {
+                    switch (c) {
+                    case 0: m0 = bits; break;
+                    case 1: m1 = bits; break;
+                    case 2: m2 = bits; break;
+                    case 3: m3 = bits; break;
+                    case 4: m4 = bits; break;
+                    case 5: m5 = bits; break;
+                    case 6: m6 = bits; break;
+                    case 7: m7 = bits; break;
+                    default: m8 = bits; break;
+                    }
+                }
                 acc.add(M.mass * part);
             }
         }
+        if (masks) {
+            const size_t n = P.n;
+            G.nbmask[k] = m0;
+            G.nbmask[n + k] = m1;
+            G.nbmask[2 * n + k] = m2;
+            G.nbmask[3 * n + k] = m3;
+            G.nbmask[4 * n + k] = m4;
+            G.nbmask[5 * n + k] = m5;
+            G.nbmask[6 * n + k] = m6;
+            G.nbmask[7 * n + k] = m7;
+            G.nbmask[8 * n + k] = m8;
+            G.nbmask[9 * n + k] = over;
+        }
         if (cnt > P.max_nb - 1) atomicOr(flags, RRSPH_FLAG_NEIGHBOUR_OVERFLOW);
         if (!cont) {
-            const double rho = (double)M.w0_density + acc.value();
-            const double pr = eos_p(P, rho);
-            G.V4[k].w = (float)rho;
-            G.PR[k] = make_float2((float)pr, (float)(pr / (rho * rho)));
-            S.rho[id] = rho;
+            // rho - rho0 = sum - (rho0 - m W(0)): the two are within a factor of two,
+            // so the float difference is exact; the Kahan and rounding residuals follow
+            const float d = ((acc.s - M.rho0_minus_w0_hi) - acc.c) - M.rho0_minus_w0_lo;
+            const float rho = M.rho0 + d;
+            const float pr = eos_pf(M, d);
+            G.V4[k].w = rho;
+            G.PR[k] = make_float2(pr, pr * __frcp_rn(rho * rho));
+            S.rho[id] = P.rho0 + (double)d;
             S.p[id] = pr;
         } else {
-            const double pr = eos_p(P, S.rho[id]);
-            const double rf = (double)G.V4[k].w;  // rho_predict, the density of the forces
-            G.PR[k] = make_float2((float)pr, (float)(pr / (rf * rf)));
+            const float d = (float)(S.rho[id] - P.rho0);
+            const float pr = eos_pf(M, d);
+            const float rf = G.V4[k].w;  // rho_predict, the density of the forces
+            G.PR[k] = make_float2(pr, pr * __frcp_rn(rf * rf));
             S.p[id] = pr;
             S.drho[id] = acc.value();
         }
@@ -181,9 +228,76 @@ __global__ void __launch_bounds__(kGatherThreads) k_density_mixed(DevParams P, S
     warp_sum_add(&scal->pairs, cnt);
 }
 
+// One pair's contribution to particle j's acceleration (and XSPH velocity):
+// update_acceleration's inner loop (UpdateAcceleration.cpp:66-97).
+template <int DIM, int SKF>
+struct ForceAcc {
+    const DevParams& P;
+    const Sorted& G;
+    float4 vj;
+    float2 prj;
+    float rhoj;
+    bool ext, intf, visc, avel, form1;
+    int intf_skf, av_skf;
+    float cax, cay, caz, cvx, cvy, cvz, arvmu;
+
+    __device__ __forceinline__ void pair(uint32_t i, float dx, float dy, float dz, float d2, int32_t ti) {
+        const MixedF& M = P.mf;
+        const float inv_dist = rsqrtf(d2);
+        const float dist = d2 * inv_dist;
+        const float q = dist * M.inv_h;
+        float m = 0.0f;  // coefficient of diff (= r_i - r_j) in this pair's acceleration
+        if (ext && ti < 0 && dist < M.lj_rr0) {
+            const float rn = M.lj_rr0 * inv_dist;
+            const float rn2 = rn * rn, rn4 = rn2 * rn2, rn8 = rn4 * rn4;
+            m -= M.lj_D * (rn8 * rn4 - rn4) * (inv_dist * inv_dist);
+        }
+        const float4 vi = G.V4[i];
+        const float rhoi = vi.w;
+        const float sc = kernel_dwdr_scalef(intf_skf, M.kf[intf_skf], q, inv_dist, M.inv_h);
+        if (intf) {
+            const float2 pri = G.PR[i];
+            float pf = form1 ? __fdividef(prj.x + pri.x, rhoj * rhoi) : (pri.y + prj.y);
+            if (P.art_pressure && (pri.x < 0 || prj.x < 0)) {
+                const float w = kernel_wf(P.ap_skf, M.kf[P.ap_skf], q);
+                const float api = pri.x < 0 ? (-M.ap_coef * pri.y) : 0.0f;
+                const float apj = prj.x < 0 ? (-M.ap_coef * prj.y) : 0.0f;
+                pf += (api + apj) * __powf(w * M.ap_inv_wdelta, M.ap_index);
+            }
+            m += sc * pf * M.mass;
+        }
+        if (visc) {
+            float vr = -((vj.x - vi.x) * dx + (vj.y - vi.y) * dy);
+            if (DIM == 3) vr -= (vj.z - vi.z) * dz;
+            if (vr < 0) {
+                const float mu = __fdividef(M.h * vr, d2 + M.etq_h2);
+                arvmu = fmaxf(arvmu, fabsf(mu));
+                const float piv = __fdividef((M.av_beta * mu - M.av_alpha_c) * mu, 0.5f * (rhoi + rhoj));
+                const float sca = (SKF || av_skf == intf_skf)
+                                      ? sc
+                                      : kernel_dwdr_scalef(av_skf, M.kf[av_skf], q, inv_dist, M.inv_h);
+                m += sca * piv * M.mass;
+            }
+        }
+        cax += dx * m;
+        cay += dy * m;
+        if (DIM == 3) caz += dz * m;
+        if (avel && ti > 0) {
+            const int sk = SKF ? SKF : P.avel_skf;
+            const float w = kernel_wf(sk, M.kf[sk], q);
+            const float mv = __fdividef(M.mass * w * M.avel_coef2, rhoi + rhoj);
+            cvx += (vi.x - vj.x) * mv;
+            cvy += (vi.y - vj.y) * mv;
+            if (DIM == 3) cvz += (vi.z - vj.z) * mv;
+        }
+    }
+};
+
 // update_acceleration (UpdateAcceleration.cpp:33-125) with the external
 // (Lennard-Jones), internal (pressure), artificial-viscosity and XSPH terms.
-template <int DIM, int SKF>
+// MASKS: iterate the neighbour bits the density pass recorded (2D) instead of
+// searching the stencil cells again.
+template <int DIM, int SKF, bool MASKS>
 __global__ void __launch_bounds__(kGatherThreads) k_forces_mixed(DevParams P, State S, Sorted G, uint32_t terms,
                                                                  StepScalars* __restrict__ scal,
                                                                  uint32_t* __restrict__ flags, int write_mu) {
@@ -194,36 +308,104 @@ __global__ void __launch_bounds__(kGatherThreads) k_forces_mixed(DevParams P, St
         const MixedF& M = P.mf;
         const uint32_t id = G.id[k];
         const float4 pj4 = G.P4[k];
-        const float4 vj = G.V4[k];
-        const float2 prj = G.PR[k];
-        const float rhoj = vj.w;
         const int32_t tj = __float_as_int(pj4.w);
+        ForceAcc<DIM, SKF> F{P, G, G.V4[k], G.PR[k], 0.0f, false, false, false, false, false, 0, 0,
+                             0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        F.rhoj = F.vj.w;
+        F.ext = (terms & RRSPH_TERM_EXTERNAL) && P.repulsive && tj > 0;
+        F.intf = terms & RRSPH_TERM_INTERNAL;
+        F.visc = (terms & RRSPH_TERM_ART_VISC) && P.art_visc;
+        F.avel = (terms & RRSPH_TERM_AVERAGE_VELOCITY) && P.avg_vel;
+        F.form1 = P.intf_form == 1;
+        F.intf_skf = SKF ? SKF : P.intf_skf;
+        F.av_skf = SKF ? SKF : P.av_skf;
         Kahan ax{0, 0}, ay{0, 0}, az{0, 0};
         Kahan avx{0, 0}, avy{0, 0}, avz{0, 0};
-        float arvmu = 0;
-        const bool ext = (terms & RRSPH_TERM_EXTERNAL) && P.repulsive && tj > 0;
-        const bool intf = terms & RRSPH_TERM_INTERNAL;
-        const bool visc = (terms & RRSPH_TERM_ART_VISC) && P.art_visc;
-        const bool avel = (terms & RRSPH_TERM_AVERAGE_VELOCITY) && P.avg_vel;
-        const bool form1 = P.intf_form == 1;
-        const int intf_skf = SKF ? SKF : P.intf_skf;
-        const int av_skf = SKF ? SKF : P.av_skf;
-        if (tj != P.type_non_existent) {
-            uint64_t cx, cy, cz;
-            decode_key<DIM>(G.key[k], cx, cy, cz);
+        if (tj != P.type_non_existent && MASKS) {
+            // the pairs recorded by the density pass, as one flat sequence over the
+            // stencil cells so that the warp runs the pair body together
+            const Stencil<DIM> st(P, G.key[k]);
+            const uint32_t over = G.nbmask[(size_t)9 * P.n + k];
+            int c = -1;
+            uint32_t bits = 0, s = 0;
+            float shx = 0.0f, shy = 0.0f;
+            for (;;) {
+                if (bits == 0) {
+                    if (c >= 0) {
+                        ax.add(F.cax);
+                        ay.add(F.cay);
+                        if (F.avel) {
+                            avx.add(F.cvx);
+                            avy.add(F.cvy);
+                        }
+                        F.cax = F.cay = F.cvx = F.cvy = 0.0f;
+                    }
+                    for (c++; c < 9; c++) {
+                        if (over & (1u << c)) continue;
+                        const uint32_t bb = G.nbmask[(size_t)c * P.n + k];
+                        if (!bb) continue;
+                        uint32_t cell;
+                        int sx, sy, sz;
+                        st.cell(c, cell, sx, sy, sz);
+                        s = G.cell_start[cell];
+                        shx = (float)sx * M.cell - pj4.x;
+                        shy = (float)sy * M.cell - pj4.y;
+                        bits = bb;
+                        break;
+                    }
+                    if (c >= 9) break;
+                }
+                const uint32_t b = __ffs(bits) - 1;
+                bits &= bits - 1;
+                const uint32_t i = s + b;
+                const float4 pi4 = G.P4[i];
+                const float dx = pi4.x + shx, dy = pi4.y + shy;
+                F.pair(i, dx, dy, 0.0f, dx * dx + dy * dy, __float_as_int(pi4.w));
+            }
+            // cells with more than 32 particles: search them
+            for (uint32_t rest = over; rest; rest &= rest - 1) {
+                const int cc = __ffs(rest) - 1;
+                uint32_t cell;
+                int sx, sy, sz;
+                if (!st.cell(cc, cell, sx, sy, sz)) continue;
+                const uint32_t s0 = G.cell_start[cell];
+                if (s0 == kEmpty) continue;
+                const uint32_t e0 = G.cell_end[cell];
+                const float hx = (float)sx * M.cell - pj4.x;
+                const float hy = (float)sy * M.cell - pj4.y;
+                F.cax = F.cay = F.cvx = F.cvy = 0.0f;
+                for (uint32_t i = s0; i < e0; i++) {
+                    if (i == k) continue;
+                    const float4 pi4 = G.P4[i];
+                    const int32_t ti = __float_as_int(pi4.w);
+                    if (ti == P.type_non_existent) continue;
+                    const float dx = pi4.x + hx, dy = pi4.y + hy;
+                    const float d2 = dx * dx + dy * dy;
+                    if (!within_cutoff<DIM>(P, G, i, k, d2)) continue;
+                    F.pair(i, dx, dy, 0.0f, d2, ti);
+                }
+                ax.add(F.cax);
+                ay.add(F.cay);
+                if (F.avel) {
+                    avx.add(F.cvx);
+                    avy.add(F.cvy);
+                }
+            }
+        } else if (tj != P.type_non_existent) {
+            const Stencil<DIM> st(P, G.key[k]);
             constexpr int NC = DIM == 3 ? 27 : 9;
 #pragma unroll 1
             for (int c = 0; c < NC; c++) {
                 uint32_t cell;
                 int sx, sy, sz;
-                if (!stencil_cell<DIM>(P, cx, cy, cz, c, cell, sx, sy, sz)) continue;
+                if (!st.cell(c, cell, sx, sy, sz)) continue;
                 const uint32_t s = G.cell_start[cell];
                 if (s == kEmpty) continue;
                 const uint32_t e = G.cell_end[cell];
                 const float shx = (float)sx * M.cell - pj4.x;
                 const float shy = (float)sy * M.cell - pj4.y;
                 const float shz = DIM == 3 ? (float)sz * M.cell - pj4.z : 0.0f;
-                float cax = 0.0f, cay = 0.0f, caz = 0.0f, cvx = 0.0f, cvy = 0.0f, cvz = 0.0f;
+                F.cax = F.cay = F.caz = F.cvx = F.cvy = F.cvz = 0.0f;
                 for (uint32_t i = s; i < e; i++) {
                     if (i == k) continue;
                     const float4 pi4 = G.P4[i];
@@ -232,60 +414,15 @@ __global__ void __launch_bounds__(kGatherThreads) k_forces_mixed(DevParams P, St
                     const float dx = pi4.x + shx, dy = pi4.y + shy, dz = DIM == 3 ? pi4.z + shz : 0.0f;
                     const float d2 = DIM == 3 ? dx * dx + dy * dy + dz * dz : dx * dx + dy * dy;
                     if (!within_cutoff<DIM>(P, G, i, k, d2)) continue;
-                    const float inv_dist = rsqrtf(d2);
-                    const float dist = d2 * inv_dist;
-                    const float q = dist * M.inv_h;
-                    float m = 0.0f;  // coefficient of diff (= r_i - r_j) in this pair's acceleration
-                    if (ext && ti < 0 && dist < M.lj_rr0) {
-                        const float rn = M.lj_rr0 * inv_dist;
-                        const float rn2 = rn * rn, rn4 = rn2 * rn2, rn8 = rn4 * rn4;
-                        m -= M.lj_D * (rn8 * rn4 - rn4) * (inv_dist * inv_dist);
-                    }
-                    const float4 vi = G.V4[i];
-                    const float rhoi = vi.w;
-                    const float sc = kernel_dwdr_scalef(intf_skf, M.kf[intf_skf], q, inv_dist, M.inv_h);
-                    if (intf) {
-                        const float2 pri = G.PR[i];
-                        float pf = form1 ? __fdividef(prj.x + pri.x, rhoj * rhoi) : (pri.y + prj.y);
-                        if (P.art_pressure && (pri.x < 0 || prj.x < 0)) {
-                            const float w = kernel_wf(P.ap_skf, M.kf[P.ap_skf], q);
-                            const float api = pri.x < 0 ? (-M.ap_coef * pri.y) : 0.0f;
-                            const float apj = prj.x < 0 ? (-M.ap_coef * prj.y) : 0.0f;
-                            pf += (api + apj) * __powf(w * M.ap_inv_wdelta, M.ap_index);
-                        }
-                        m += sc * pf * M.mass;
-                    }
-                    if (visc) {
-                        float vr = -((vj.x - vi.x) * dx + (vj.y - vi.y) * dy);
-                        if (DIM == 3) vr -= (vj.z - vi.z) * dz;
-                        if (vr < 0) {
-                            const float mu = __fdividef(M.h * vr, d2 + M.etq_h2);
-                            arvmu = fmaxf(arvmu, fabsf(mu));
-                            const float piv = __fdividef((M.av_beta * mu - M.av_alpha_c) * mu, 0.5f * (rhoi + rhoj));
-                            const float sca = (SKF || av_skf == intf_skf)
-                                                  ? sc
-                                                  : kernel_dwdr_scalef(av_skf, M.kf[av_skf], q, inv_dist, M.inv_h);
-                            m += sca * piv * M.mass;
-                        }
-                    }
-                    cax += dx * m;
-                    cay += dy * m;
-                    if (DIM == 3) caz += dz * m;
-                    if (avel && ti > 0) {
-                        const float w = kernel_wf(SKF ? SKF : P.avel_skf, M.kf[SKF ? SKF : P.avel_skf], q);
-                        const float mv = __fdividef(M.mass * w * M.avel_coef2, rhoi + rhoj);
-                        cvx += (vi.x - vj.x) * mv;
-                        cvy += (vi.y - vj.y) * mv;
-                        if (DIM == 3) cvz += (vi.z - vj.z) * mv;
-                    }
+                    F.pair(i, dx, dy, dz, d2, ti);
                 }
-                ax.add(cax);
-                ay.add(cay);
-                if (DIM == 3) az.add(caz);
-                if (avel) {
-                    avx.add(cvx);
-                    avy.add(cvy);
-                    if (DIM == 3) avz.add(cvz);
+                ax.add(F.cax);
+                ay.add(F.cay);
+                if (DIM == 3) az.add(F.caz);
+                if (F.avel) {
+                    avx.add(F.cvx);
+                    avy.add(F.cvy);
+                    if (DIM == 3) avz.add(F.cvz);
                 }
             }
         }
@@ -294,12 +431,12 @@ __global__ void __launch_bounds__(kGatherThreads) k_forces_mixed(DevParams P, St
         S.ax[id] = axd;
         S.ay[id] = ayd;
         if (DIM == 3) S.az[id] = azd;
-        if (avel) {
+        if (F.avel) {
             S.avx[id] = avx.value();
             S.avy[id] = avy.value();
             if (DIM == 3) S.avz[id] = avz.value();
         }
-        arvmu_d = arvmu;
+        arvmu_d = F.arvmu;
         if (write_mu) S.mu[id] = arvmu_d;
         if (P.dt_reduce) amag = sqrt(axd * axd + ayd * ayd + azd * azd);
     }
@@ -320,10 +457,16 @@ void launch_density_mixed(const DevParams& P, const State& S, const Sorted& G, S
 }
 template <int DIM>
 void launch_forces_mixed(const DevParams& P, const State& S, const Sorted& G, uint32_t terms, StepScalars* scal,
-                         uint32_t* flags, int write_mu, cudaStream_t st) {
+                         uint32_t* flags, int write_mu, int use_masks, cudaStream_t st) {
     const unsigned blocks = (P.n + kGatherThreads - 1) / kGatherThreads;
-    if (P.all_cubic) k_forces_mixed<DIM, 1><<<blocks, kGatherThreads, 0, st>>>(P, S, G, terms, scal, flags, write_mu);
-    else k_forces_mixed<DIM, 0><<<blocks, kGatherThreads, 0, st>>>(P, S, G, terms, scal, flags, write_mu);
+    const bool m = DIM == 2 && use_masks && G.nbmask != nullptr;
+    if (P.all_cubic) {
+        if (m) k_forces_mixed<DIM, 1, true><<<blocks, kGatherThreads, 0, st>>>(P, S, G, terms, scal, flags, write_mu);
+        else k_forces_mixed<DIM, 1, false><<<blocks, kGatherThreads, 0, st>>>(P, S, G, terms, scal, flags, write_mu);
+    } else {
+        if (m) k_forces_mixed<DIM, 0, true><<<blocks, kGatherThreads, 0, st>>>(P, S, G, terms, scal, flags, write_mu);
+        else k_forces_mixed<DIM, 0, false><<<blocks, kGatherThreads, 0, st>>>(P, S, G, terms, scal, flags, write_mu);
+    }
 }
 
 template void launch_density_mixed<2>(const DevParams&, const State&, const Sorted&, StepScalars*, uint32_t*,
@@ -331,8 +474,8 @@ template void launch_density_mixed<2>(const DevParams&, const State&, const Sort
 template void launch_density_mixed<3>(const DevParams&, const State&, const Sorted&, StepScalars*, uint32_t*,
                                       cudaStream_t);
 template void launch_forces_mixed<2>(const DevParams&, const State&, const Sorted&, uint32_t, StepScalars*, uint32_t*,
-                                     int, cudaStream_t);
+                                     int, int, cudaStream_t);
 template void launch_forces_mixed<3>(const DevParams&, const State&, const Sorted&, uint32_t, StepScalars*, uint32_t*,
-                                     int, cudaStream_t);
+                                     int, int, cudaStream_t);
 
 }  // namespace rrsph

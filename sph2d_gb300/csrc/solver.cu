@@ -54,6 +54,7 @@ struct rrsph_solver {
     unsigned long long launches = 0;
     unsigned long long launches_in_graph[2] = {0, 0};
     uint64_t step_index = 0;
+    bool keys_ready = false;  // the next step's predict + keys were computed by the last whole step
     bool timing = false;
     cudaEvent_t ev[kPhases + 1] = {};
     double phase_ms[kPhases] = {};
@@ -182,6 +183,13 @@ int fill_dev_params(const rrsph_params& p, rrsph::DevParams& P) {
     M.cut2_hi = (float)(P.cut2 * (1.0 + 1e-5));
     for (int k = 0; k < 5; k++) M.kf[k] = (float)P.kf[k];
     M.w0_density = (float)(P.mass * P.w0_density);
+    {
+        const double d = P.rho0 - P.mass * P.w0_density;
+        M.rho0_minus_w0_hi = (float)d;
+        M.rho0_minus_w0_lo = (float)(d - (double)M.rho0_minus_w0_hi);
+    }
+    M.B = (float)P.B;
+    M.inv_rho0 = (float)(1.0 / P.rho0);
     M.lj_rr0 = (float)P.lj_rr0;
     M.lj_D = (float)P.lj_D;
     M.etq_h2 = (float)P.etq_h2;
@@ -227,22 +235,28 @@ void enqueue_density(rrsph_solver* s, rrsph::StepScalars* scal) {
 }
 
 template <int DIM>
-void enqueue_forces(rrsph_solver* s, uint32_t terms, rrsph::StepScalars* scal, int write_mu) {
+void enqueue_forces(rrsph_solver* s, uint32_t terms, rrsph::StepScalars* scal, int write_mu, int use_masks = 0) {
     if (s->precision == RRSPH_PRECISION_MIXED)
-        rrsph::launch_forces_mixed<DIM>(s->P, s->S, s->G, terms, scal, s->flags, write_mu, s->stream);
+        rrsph::launch_forces_mixed<DIM>(s->P, s->S, s->G, terms, scal, s->flags, write_mu, use_masks, s->stream);
     else rrsph::launch_forces_fp64<DIM>(s->P, s->S, s->G, terms, scal, s->flags, write_mu, s->stream);
     s->launches++;
 }
 
-// One loop step on parity `par`; events[i] (if non-null) are recorded between phases.
+// One loop step on parity `par`; events[i] (if non-null) are recorded between
+// phases. with_keys runs the predict + key pass first; otherwise the previous
+// step's whole-step kernel has done it. The whole-step kernel always prepares
+// the next step's predict + keys.
 template <int DIM>
-void enqueue_step(rrsph_solver* s, int par, cudaEvent_t* events) {
+void enqueue_step(rrsph_solver* s, int par, cudaEvent_t* events, bool with_keys) {
     rrsph::StepScalars* cur = s->scal + par;
     rrsph::StepScalars* nxt = s->scal + (par ^ 1);
     const bool cont = s->P.density_treatment != 0;
     rrsph::GatherSrc fsrc{s->S.vpx, s->S.vpy, s->S.vpz, cont ? s->S.rho_pred : s->S.rho, nullptr};
     if (events) cudaEventRecord(events[0], s->stream);
-    rrsph::launch_keys<DIM>(s->P, s->S, s->G, cur, 1, s->flags, s->stream);
+    if (with_keys) {
+        rrsph::launch_keys<DIM>(s->P, s->S, s->G, cur, 1, s->flags, s->stream);
+        s->launches++;
+    }
     if (events) cudaEventRecord(events[1], s->stream);
     rrsph::radix_sort_pairs(s->G.keys_in, s->G.ids_in, s->G.keys_a, s->G.ids_a, s->G.sort_scratch, s->P.n,
                             s->sort_bits, s->stream, &s->G.key, &s->G.id, &s->launches);
@@ -251,16 +265,22 @@ void enqueue_step(rrsph_solver* s, int par, cudaEvent_t* events) {
     if (events) cudaEventRecord(events[3], s->stream);
     enqueue_density<DIM>(s, cur);
     if (events) cudaEventRecord(events[4], s->stream);
-    enqueue_forces<DIM>(s, RRSPH_TERM_ALL, cur, 0);
+    enqueue_forces<DIM>(s, RRSPH_TERM_ALL, cur, 0, 1);
     if (events) cudaEventRecord(events[5], s->stream);
-    rrsph::launch_whole_step<DIM>(s->P, s->S, cur, nxt, s->flags, s->stream);
+    rrsph::launch_whole_step<DIM>(s->P, s->S, s->G, cur, nxt, s->flags, 1, s->stream);
     if (events) cudaEventRecord(events[6], s->stream);
-    s->launches += 3;
+    s->launches += 2;
 }
 
-void enqueue_step_dim(rrsph_solver* s, int par, cudaEvent_t* events) {
-    if (s->dim == 3) enqueue_step<3>(s, par, events);
-    else enqueue_step<2>(s, par, events);
+void enqueue_step_dim(rrsph_solver* s, int par, cudaEvent_t* events, bool with_keys) {
+    if (s->dim == 3) enqueue_step<3>(s, par, events, with_keys);
+    else enqueue_step<2>(s, par, events, with_keys);
+}
+
+void enqueue_keys_dim(rrsph_solver* s, int par) {
+    if (s->dim == 3) rrsph::launch_keys<3>(s->P, s->S, s->G, s->scal + par, 1, s->flags, s->stream);
+    else rrsph::launch_keys<2>(s->P, s->S, s->G, s->scal + par, 1, s->flags, s->stream);
+    s->launches++;
 }
 
 int ensure_staging(rrsph_solver* s, size_t words) {
@@ -278,6 +298,10 @@ int ensure_staging(rrsph_solver* s, size_t words) {
 }
 
 int flags_to_status(const rrsph_solver* s, uint32_t f) {
+    // the per-step bounds check of update_step comes before the next step's grid
+    // find, whose key pass the whole-step kernel already ran
+    if ((f & RRSPH_FLAG_OUTSIDE_GEOMETRY) && s->params.consistency_check && s->params.consistency_treatment == 1)
+        return set_error(RRSPH_ERR_OUTSIDE_GEOMETRY, "Encounter particle outside boundaries");
     if (f & RRSPH_FLAG_OUT_OF_DOMAIN) return set_error(RRSPH_ERR_OUT_OF_DOMAIN, "cell_idx was >= params.max_cells");
     if (f & RRSPH_FLAG_NEIGHBOUR_OVERFLOW) return set_error(RRSPH_ERR_NEIGHBOUR_OVERFLOW, "making neighbours grid: error occured");
     if (f & kFlagNeverEnding) return set_error(RRSPH_ERR_NEVER_ENDING, "never ending simulation");
@@ -343,6 +367,7 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
         if (cont) { A(G.vdx, n); A(G.vdy, n); if (d3) A(G.vdz, n); A(G.rhod, n); }
     } else {
         A(G.P4, n); A(G.V4, n); A(G.PR, n);
+        if (!d3) A(G.nbmask, 10 * n);
         if (cont) A(G.VD4, n);
     }
     A(s->scal, 2);
@@ -425,6 +450,7 @@ extern "C" int rrsph_upload(rrsph_solver* s, const double* r, uint32_t stride, c
     RRSPH_CUDA_TRY(cudaMemcpyAsync(s->scal, s->h_scal, sizeof(init), cudaMemcpyHostToDevice, st));
     RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
     s->step_index = 0;
+    s->keys_ready = false;
     return RRSPH_OK;
 }
 
@@ -456,8 +482,10 @@ int enqueue_steps(rrsph_solver* s, uint64_t nsteps) {
     cudaStream_t st = s->stream;
     for (uint64_t k = 0; k < nsteps; k++) {
         const int par = (int)(s->step_index & 1);
+        const bool with_keys = !s->keys_ready;
+        s->keys_ready = true;
         if (s->timing) {
-            enqueue_step_dim(s, par, s->ev);
+            enqueue_step_dim(s, par, s->ev, with_keys);
             RRSPH_CUDA_TRY(cudaEventSynchronize(s->ev[kPhases]));
             for (int i = 0; i < kPhases; i++) {
                 float ms = 0;
@@ -470,7 +498,7 @@ int enqueue_steps(rrsph_solver* s, uint64_t nsteps) {
                 cudaGraph_t g = nullptr;
                 const unsigned long long before = s->launches;
                 RRSPH_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-                enqueue_step_dim(s, par, nullptr);
+                enqueue_step_dim(s, par, nullptr, false);
                 RRSPH_CUDA_TRY(cudaStreamEndCapture(st, &g));
                 const cudaError_t e = cudaGraphInstantiate(&s->graph[par], g, 0);
                 cudaGraphDestroy(g);
@@ -478,10 +506,11 @@ int enqueue_steps(rrsph_solver* s, uint64_t nsteps) {
                 s->launches_in_graph[par] = s->launches - before;
                 s->launches = before;
             }
+            if (with_keys) enqueue_keys_dim(s, par);
             RRSPH_CUDA_TRY(cudaGraphLaunch(s->graph[par], st));
             s->launches += s->launches_in_graph[par];
         } else {
-            enqueue_step_dim(s, par, nullptr);
+            enqueue_step_dim(s, par, nullptr, with_keys);
         }
         s->step_index++;
     }
@@ -574,6 +603,7 @@ namespace {
 
 template <int DIM>
 void enqueue_component_grid(rrsph_solver* s, bool with_p) {
+    s->keys_ready = false;  // this grid's keys were made without the predictor
     rrsph::GatherSrc fsrc{s->S.vx, s->S.vy, s->S.vz, s->S.rho, with_p ? s->S.p : nullptr};
     enqueue_grid<DIM>(s, 0, s->scal, fsrc);
 }

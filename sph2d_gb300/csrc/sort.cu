@@ -11,7 +11,7 @@
 //   2. k_digit_scan:  one warp per digit scans its row over tiles (exclusive)
 //                     and records the digit total
 //   3. k_scatter:     each tile ranks its keys stably (warp match + per-warp
-//                     counts, in (round, warp, lane) = input order) and writes
+//                     counts, in (warp, round, lane) = input order) and writes
 //                     them to total-prefix[d] + tile-prefix[d][tile] + rank.
 #include "sort.cuh"
 
@@ -69,19 +69,25 @@ __global__ void k_digit_scan(uint32_t* __restrict__ counts, uint32_t tiles, uint
     if (lane == 0) totals[warp] = carry;
 }
 
+// Stable scatter of one tile. Each warp owns 256 consecutive keys of the tile
+// (kSortItems rounds of 32), so the tile's input order is (warp, round, lane):
+// a key's rank is the count of equal digits before it in its warp (per-warp
+// running counts, updated by one leader per digit group and round), plus the
+// counts of that digit in the warps before it, plus the digit's start for
+// this tile. Three block barriers per tile.
 __global__ void __launch_bounds__(kSortThreads) k_scatter(const uint32_t* __restrict__ keys_in,
                                                           const uint32_t* __restrict__ vals_in,
                                                           uint32_t* __restrict__ keys_out,
                                                           uint32_t* __restrict__ vals_out, uint32_t n, int shift,
                                                           uint32_t tiles, const uint32_t* __restrict__ prefix,
                                                           const uint32_t* __restrict__ totals) {
-    __shared__ uint32_t base_of[kRadix];   // output start of each digit for this tile
-    __shared__ uint32_t running[kRadix];   // keys of each digit already placed by earlier rounds
-    __shared__ uint32_t wcount[kWarps][kRadix];
-    __shared__ uint32_t scan_tmp[kRadix];
+    __shared__ uint32_t base_of[kRadix];                // output start of each digit for this tile
+    __shared__ uint16_t wcnt[kWarps][kRadix];           // per-warp digit counts, then per-warp offsets
+    __shared__ uint32_t scan_tmp[kWarps];
 
     const int tid = threadIdx.x;
     const uint32_t warp = tid >> 5, lane = tid & 31;
+    for (int i = tid; i < kWarps * kRadix / 2; i += kSortThreads) reinterpret_cast<uint32_t*>(&wcnt[0][0])[i] = 0;
     // exclusive scan of the 256 digit totals (kSortThreads == kRadix)
     {
         const uint32_t v = totals[tid];
@@ -96,40 +102,42 @@ __global__ void __launch_bounds__(kSortThreads) k_scatter(const uint32_t* __rest
         uint32_t warp_off = 0;
         for (uint32_t w = 0; w < warp; w++) warp_off += scan_tmp[w];
         base_of[tid] = warp_off + incl - v + prefix[(size_t)tid * tiles + blockIdx.x];
-        running[tid] = 0;
+    }
+    uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
+    const uint32_t wbase = blockIdx.x * (uint32_t)kSortTile + warp * (kSortItems * 32);
+    const uint32_t lt = lanemask_lt();
+#pragma unroll
+    for (int r = 0; r < kSortItems; r++) {
+        const uint32_t idx = wbase + r * 32 + lane;
+        const bool valid = idx < n;
+        key[r] = valid ? keys_in[idx] : 0u;
+        val[r] = valid ? vals_in[idx] : 0u;
+        const uint32_t d = valid ? ((key[r] >> shift) & (kRadix - 1)) : kRadix;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        const uint32_t cur = valid ? wcnt[warp][d] : 0u;
+        __syncwarp();
+        if (valid && (__ffs(peers) - 1) == (int)lane) wcnt[warp][d] = (uint16_t)(cur + __popc(peers));
+        __syncwarp();
+        rank[r] = valid ? cur + __popc(peers & lt) : 0xFFFFFFFFu;
     }
     __syncthreads();
-
-    const uint32_t base = blockIdx.x * (uint32_t)kSortTile;
-    for (int r = 0; r < kSortItems; r++) {
-        const uint32_t idx = base + r * kSortThreads + tid;
-        const bool valid = idx < n;
-        uint32_t key = 0, val = 0, d = kRadix;
-        if (valid) {
-            key = keys_in[idx];
-            val = vals_in[idx];
-            d = (key >> shift) & (kRadix - 1);
-        }
-        for (int i = tid; i < kWarps * kRadix; i += kSortThreads) (&wcount[0][0])[i] = 0;
-        __syncthreads();
-        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
-        const uint32_t rank = __popc(peers & lanemask_lt());
-        if (valid && rank == 0) wcount[warp][d] = __popc(peers);
-        __syncthreads();
-        if (valid) {
-            uint32_t pos = base_of[d] + running[d] + rank;
-            for (uint32_t w = 0; w < warp; w++) pos += wcount[w][d];
-            keys_out[pos] = key;
-            vals_out[pos] = val;
-        }
-        __syncthreads();
-        {
-            uint32_t s = 0;
+    {   // per digit: counts of the warps -> exclusive offsets over warps
+        uint32_t run = 0;
 #pragma unroll
-            for (int w = 0; w < kWarps; w++) s += wcount[w][tid];
-            running[tid] += s;
+        for (int w = 0; w < kWarps; w++) {
+            const uint32_t c = wcnt[w][tid];
+            wcnt[w][tid] = (uint16_t)run;
+            run += c;
         }
-        __syncthreads();
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kSortItems; r++) {
+        if (rank[r] == 0xFFFFFFFFu) continue;
+        const uint32_t d = (key[r] >> shift) & (kRadix - 1);
+        const uint32_t pos = base_of[d] + wcnt[warp][d] + rank[r];
+        keys_out[pos] = key[r];
+        vals_out[pos] = val[r];
     }
 }
 
