@@ -227,6 +227,19 @@ int rrsph_set_time(rrsph_solver* s, double time);
  * stay set (rrsph_status reads and clears them; rrsph_step clears them when
  * it starts). */
 int rrsph_sync(rrsph_solver* s, double* time_out);
+/* The time loop with the layer output of RRSPHOutput (TimeIntegration.cpp:53-100,
+ * Output.cpp:28-79, 223-446), from the uploaded state at *time_io until time
+ * exceeds simulation_time or max_steps steps ran: writes
+ * <dir>/data/<t>.csv at the start and whenever time - last_save > save_time
+ * (every step with save_every_step), <dir>/dump/<t>.csv when use_dump and
+ * time - last_dump > dump_time, and <dir>/crash_dump_<t>.csv when a
+ * CONSISTENCY_STOP bounds check fails (use_crash_dump), then returns its
+ * error. Names use the reference's time formatting (TimeFormat.cpp:36-53).
+ * Layers are formatted on writer threads while the GPU keeps stepping; the
+ * call returns after every file is written. *steps_done (may be NULL)
+ * receives the number of steps run. */
+int rrsph_run(rrsph_solver* s, const char* experiment_dir, double* time_io,
+              uint64_t max_steps, uint64_t* steps_done);
 /* Sticky RRSPH_FLAG_* bits raised by device checks since the last clear. */
 int rrsph_status(rrsph_solver* s, uint32_t* flags, int clear);
 /* Directed neighbour pairs (the entries find_neighbours would list) of the

@@ -26,12 +26,14 @@ CSRC = PKG / "csrc"
 HOST = PKG / "host"
 BUILD = PKG / "_build"
 LIB = PKG / "librrsph_cuda.so"
+RUNNER = PKG / "rrsph_run"
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_LIB = ORACLE_DIR / "liboracle.so"
 REF_BIN = ORACLE_DIR / "_ref" / "rrsph_ref"
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CU_SOURCES = ["sort.cu", "kernels_common.cu", "kernels_fp64.cu", "kernels_mixed.cu", "solver.cu", "sort_noalloc.cu"]
+CU_SOURCES = ["sort.cu", "kernels_common.cu", "kernels_fp64.cu", "kernels_mixed.cu", "solver.cu", "sort_noalloc.cu",
+              "run_loop.cu"]
 CPP_SOURCES = ["params.cpp", "layers.cpp"]
 
 
@@ -97,6 +99,11 @@ def build_cuda(verbose: bool = False, extra_nvcc=()) -> Path:
         tmp = LIB.with_suffix(".so.tmp")
         _run([nvcc, ARCH, "-shared", "-o", tmp, *objs, "-lcudart_static", "-lrt", "-ldl", "-lpthread"], verbose)
         os.replace(tmp, LIB)
+    # the command-line runner (links the library, found next to it at run time)
+    main_src = HOST / "rrsph_run_main.cpp"
+    if not _newer(RUNNER, [main_src, LIB, ROOT / "include" / "rrsph_cuda.h"]):
+        _run(["g++", "-O2", "-std=c++17", "-Wall", "-o", RUNNER, main_src, "-L", PKG, "-lrrsph_cuda",
+              "-Wl,-rpath,$ORIGIN"], verbose)
     return LIB
 
 

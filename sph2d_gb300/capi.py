@@ -126,6 +126,7 @@ _SIGS = {
     "rrsph_step_async": (C.c_int, [C.c_void_p, C.c_uint64]),
     "rrsph_set_time": (C.c_int, [C.c_void_p, C.c_double]),
     "rrsph_sync": (C.c_int, [C.c_void_p, _dp]),
+    "rrsph_run": (C.c_int, [C.c_void_p, C.c_char_p, _dp, C.c_uint64, _P(C.c_uint64)]),
     "rrsph_status": (C.c_int, [C.c_void_p, _u32p, C.c_int]),
     "rrsph_get_dt": (C.c_int, [C.c_void_p, _dp]),
     "rrsph_pair_count": (C.c_int, [C.c_void_p, _P(C.c_uint64), _P(C.c_uint64)]),

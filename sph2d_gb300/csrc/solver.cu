@@ -23,43 +23,7 @@
 
 using rrsph::set_error;
 
-namespace {
-
-constexpr int kPhases = 6;
-const char* const kPhaseNames[kPhases] = {"keys", "sort", "reorder", "density", "forces", "whole"};
-constexpr uint32_t kFlagNeverEnding = RRSPH_FLAG_NEVER_ENDING;
-
-}  // namespace
-
-struct rrsph_solver {
-    rrsph_params params{};
-    rrsph::DevParams P{};
-    int precision = RRSPH_PRECISION_FP64;
-    int dim = 2;
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    rrsph::State S{};
-    rrsph::Sorted G{};
-    rrsph::StepScalars* scal = nullptr;  // [2] on the device
-    uint32_t* flags = nullptr;
-    rrsph::StepScalars* h_scal = nullptr;  // pinned
-    uint32_t* h_flags = nullptr;           // pinned
-    double* h_time = nullptr;              // pinned
-    double* staging = nullptr;
-    size_t staging_words = 0;
-    std::vector<void*> allocations;
-    int sort_bits = 0;
-    bool graphs = true;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    unsigned long long launches = 0;
-    unsigned long long launches_in_graph[2] = {0, 0};
-    uint64_t step_index = 0;
-    bool keys_ready = false;  // the next step's predict + keys were computed by the last whole step
-    bool timing = false;
-    cudaEvent_t ev[kPhases + 1] = {};
-    double phase_ms[kPhases] = {};
-    uint64_t timed_steps = 0;
-};
+#include "solver_impl.cuh"
 
 namespace {
 

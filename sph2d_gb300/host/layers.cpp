@@ -8,6 +8,7 @@
 #include "../../include/rrsph_cuda.h"
 #include "error.hpp"
 
+#include <charconv>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -19,11 +20,17 @@ using rrsph::set_error;
 
 namespace {
 
-// std::to_string(double) is specified as printf("%f")
+// std::to_string(double) is specified as printf("%f"); std::to_chars with
+// fixed format and precision 6 produces the same characters, faster.
 void put_f(std::string& out, double v) {
     char buf[512];
-    const int n = std::snprintf(buf, sizeof(buf), "%f", v);
-    out.append(buf, (size_t)(n > 0 ? n : 0));
+    const auto res = std::to_chars(buf, buf + sizeof(buf), v, std::chars_format::fixed, 6);
+    if (res.ec == std::errc()) {
+        out.append(buf, (size_t)(res.ptr - buf));
+    } else {
+        const int n = std::snprintf(buf, sizeof(buf), "%f", v);
+        out.append(buf, (size_t)(n > 0 ? n : 0));
+    }
 }
 
 }  // namespace

@@ -148,6 +148,13 @@ class Solver:
         check(lib().rrsph_step(self._h, nsteps, C.byref(t)))
         return t.value
 
+    def run(self, experiment_dir, time: float = 0.0, max_steps: int = 2**63 - 1):
+        """The loop with layer output (rrsph_run); returns (time, steps)."""
+        t = C.c_double(time)
+        n = C.c_uint64()
+        check(lib().rrsph_run(self._h, str(experiment_dir).encode(), C.byref(t), max_steps, C.byref(n)))
+        return t.value, int(n.value)
+
     def step_async(self, nsteps: int) -> None:
         check(lib().rrsph_step_async(self._h, nsteps))
 

@@ -191,3 +191,22 @@ def test_experiment_directory_round_trip(tmp_path):
     for name in ("hsml", "mass", "max_cells", "dt", "nwm_freq", "nwm_wave_number", "eos_sound_vel"):
         assert getattr(p, name) == pytest.approx(getattr(q, name), rel=1e-12), name
     assert json.loads((tmp_path / "ModelParams.json").read_text())["nwm"] == 2
+
+
+def test_layer_numbers_format_like_printf(tmp_path):
+    """Layer values must print exactly as std::to_string (printf "%f")."""
+    from sph2d_gb300 import cases, write_layer
+
+    case = cases.dam_break_2d(nx=10, ny=10)
+    p = case.params()
+    n = case.ntotal
+    rng = np.random.default_rng(3)
+    specials = np.array([0.0078125, -0.0078125, 2.5e-7, 0.5e-6, 123456789.123456789, -1e-9, 1e15 + 0.5, 0.1, 0.3])
+    vals = np.concatenate([specials, rng.normal(0, 10, n - len(specials)) * 10.0 ** rng.integers(-8, 8, n - len(specials))])
+    r = np.stack([vals, -vals[::-1]], axis=1)
+    write_layer(tmp_path / "x.csv", p, r, r, vals, vals, case.itype, dump=True)
+    lines = (tmp_path / "x.csv").read_text().splitlines()[1:]
+    for i, line in enumerate(lines):
+        f = line.split(",")
+        assert f[0] == "%f" % r[i, 0] and f[1] == "%f" % r[i, 1], (i, f[:2], r[i])
+        assert f[5] == "%f" % vals[i]
