@@ -295,6 +295,48 @@ int rrsph_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* ids_in,
                              uint32_t* keys_out, uint32_t* ids_out, uint32_t n,
                              uint32_t key_bits, void* stream);
 
+/* ---- piston optimisation: Fourier piston and the adjoint of the loop -------- */
+/* Maximum number of Fourier coefficients of rrsph_set_piston_fourier. */
+#define RRSPH_PISTON_FOURIER_MAX 16
+/* Replaces the velocity law of the piston (nwm == 2, dynamic_boundaries,
+ * WaveMaker.cpp:34-82) by the displacement X(t) = sum_k coef[k-1] sin(k omega t),
+ * k = 1..ncoef: every step the particles [nwm_particles_start,
+ * nwm_particles_end) get v.x = X'(t) and r.x += X'(t) dt, as the reference's
+ * piston does with its own law. ncoef = 0 restores the reference's law.
+ * RRSPH_ERR_UNSUPPORTED unless nwm == 2. */
+int rrsph_set_piston_fourier(rrsph_solver* s, uint32_t ncoef, double omega, const double* coef);
+
+/* A forward run recorded for rrsph_adjoint_reverse. The gauge is the
+ * reference's maxInLayer (tools/WaterProfile/include/HeightTesting.h:25-54):
+ * the largest y > 0 over particles of itype == gauge_type (0: any) with
+ * |x - gauge_x| < gauge_search_n * hsml, sampled on the states after
+ * sample_from, sample_from + sample_every, ... <= nsteps steps. */
+typedef struct rrsph_adjoint_config {
+    uint32_t struct_size;        /* sizeof(rrsph_adjoint_config) */
+    uint32_t checkpoint_every;   /* K >= 1: the state is stored every K steps, the steps in between are recomputed */
+    uint64_t nsteps;
+    double gauge_x;
+    double gauge_search_n;
+    int32_t gauge_type;
+    uint32_t sample_every;       /* >= 1 */
+    uint64_t sample_from;
+} rrsph_adjoint_config;
+
+/* Runs cfg->nsteps steps of the FP64 loop from the uploaded state at *time_io,
+ * storing checkpoints, and returns the gauge series (gauges[s], s <
+ * *nsamples <= max_samples). Method set: FP64 solver, 2D, summation density,
+ * cubic kernel, no artificial pressure / XSPH, constant dt, no wall-disappear
+ * wave maker; otherwise RRSPH_ERR_UNSUPPORTED. */
+int rrsph_adjoint_forward(rrsph_solver* s, const rrsph_adjoint_config* cfg, double* time_io, double* gauges,
+                          uint64_t max_samples, uint64_t* nsamples);
+/* Reverse sweep of the last rrsph_adjoint_forward: given dL/dgauge[s], returns
+ * dL/dcoef[k] of the Fourier piston (dcoef may be NULL; ncoef entries) and
+ * dL/d(piston velocity of step n) (dpiston_vx may be NULL; nsteps entries).
+ * Each step's adjoint is a gather over the step's neighbour pairs (recomputed
+ * from the checkpoints; no atomics). The solver's state afterwards is the
+ * state at the end of the forward run. */
+int rrsph_adjoint_reverse(rrsph_solver* s, const double* dgauges, double* dcoef, double* dpiston_vx);
+
 /* ---- timing hooks for benchmarks ------------------------------------------ */
 /* Number of kernel phases one step launches and their names. */
 int rrsph_phase_count(rrsph_solver* s, int* count);

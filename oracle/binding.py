@@ -78,6 +78,10 @@ def lib() -> C.CDLL:
             "orc_run": (C.c_int, [_pp, _dp, _dp, C.c_uint32, _dp, _dp, _i32p, _dp, _dp, C.c_uint64, C.c_uint64, _dp,
                                   C.POINTER(C.c_uint64)]),
             "orc_gauge": (C.c_double, [_pp, _dp, C.c_uint32, _i32p, C.c_double, C.c_double, C.c_int32]),
+            "orc_piston_tangent_run": (C.c_int, [_pp, _dp, _dp, C.c_uint32, _dp, _dp, _i32p, _dp, C.c_uint64, _dp,
+                                                 C.c_uint32, C.c_double, _dp, C.c_double, C.c_double, C.c_int32,
+                                                 C.c_uint64, C.c_uint64, _dp, _dp, C.c_uint64,
+                                                 C.POINTER(C.c_uint64)]),
             "orc_set_threads": (None, [C.c_int]),
             "orc_get_threads": (C.c_int, []),
         }
@@ -187,6 +191,33 @@ def run(p: RrsphParams, r, v, rho, itype, nsteps: int, time: float = 0.0, pres=N
                        nsteps, C.byref(t), C.byref(pairs)))
     return {"r": r, "v": v, "rho": rho, "p": pres, "itype": itype, "a": a, "drho": drho, "time": t.value,
             "pairs": int(pairs.value)}
+
+
+def piston_tangent_run(p: RrsphParams, r, v, rho, itype, nsteps: int, omega: float, coef, gauge_x: float,
+                       search_n: float = 3.0, gauge_type: int = 2, sample_from: int = 0, sample_every: int = 1,
+                       time: float = 0.0):
+    """Forward run with the Fourier piston X(t) = sum_k coef[k-1] sin(k omega t)
+    and the forward-mode derivatives of the gauge series by the coefficients.
+    Returns (gauges[ns], dgauges[ns, ncoef], state dict)."""
+    q = p.copy()
+    r = np.array(r, dtype=np.float64, order="C")
+    v = np.array(v, dtype=np.float64, order="C")
+    rho = np.array(rho, dtype=np.float64)
+    itype = np.array(itype, dtype=np.int32)
+    n, dim = r.shape
+    coef = np.ascontiguousarray(coef, dtype=np.float64)
+    pres = np.zeros(n)
+    a = np.zeros((n, dim))
+    cap = (nsteps - sample_from) // sample_every + 1 if nsteps >= sample_from else 0
+    g = np.zeros(max(cap, 1))
+    dg = np.zeros((max(cap, 1), coef.size))
+    t = C.c_double(time)
+    ns = C.c_uint64()
+    _chk(lib().orc_piston_tangent_run(C.byref(q), _d(r), _d(v), dim, _d(rho), _d(pres), _i(itype), _d(a), nsteps,
+                                      C.byref(t), coef.size, float(omega), _d(coef), float(gauge_x), float(search_n),
+                                      int(gauge_type), sample_from, sample_every, _d(g), _d(dg), cap, C.byref(ns)))
+    k = int(ns.value)
+    return g[:k], dg[:k], {"r": r, "v": v, "rho": rho, "p": pres, "itype": itype, "a": a, "time": t.value}
 
 
 def gauge(p: RrsphParams, r, itype, x: float, search_n: float = 3.0, type_filter: int = 0) -> float:

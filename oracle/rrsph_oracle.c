@@ -630,12 +630,13 @@ int orc_run(rrsph_params* p, double* r, double* v, uint32_t stride, double* rho,
     double* v_pred = (double*)malloc(n * stride * sizeof(double));
     double* rho_pred = (double*)malloc(n * sizeof(double));
     double* av = (double*)calloc(n * stride, sizeof(double));
+    double* mu = (double*)calloc(n, sizeof(double));
     uint32_t* keys = (uint32_t*)malloc(n * sizeof(uint32_t));
     uint32_t* grid = (uint32_t*)malloc(n * sizeof(uint32_t));
     uint32_t* cells = (uint32_t*)malloc((p->max_cells + 1) * sizeof(uint32_t));
     uint32_t* counts = (uint32_t*)malloc(n * sizeof(uint32_t));
     uint32_t* list = (uint32_t*)malloc(n * (size_t)max_per * sizeof(uint32_t));
-    if (!v_pred || !rho_pred || !av || !keys || !grid || !cells || !counts || !list) {
+    if (!v_pred || !rho_pred || !av || !mu || !keys || !grid || !cells || !counts || !list) {
         rc = RRSPH_ERR_OUT_OF_MEMORY;
         goto done;
     }
@@ -666,7 +667,28 @@ int orc_run(rrsph_params* p, double* r, double* v, uint32_t stride, double* rho,
         else orc_density_sum(p, r, stride, counts, list, max_per, rho, pres);
         /* update_acceleration: v_predict, rho_predict (continuity) or rho */
         orc_forces(p, RRSPH_TERM_ALL, itype, r, v_pred, stride, cont ? rho_pred : rho, pres,
-                   counts, list, max_per, a, p->average_velocity ? av : NULL, NULL);
+                   counts, list, max_per, a, p->average_velocity ? av : NULL, mu);
+        /* update_dt (UpdateAcceleration.cpp:15-29, 104-121) under DT_CORRECTION_DYNAMIC:
+         * the OpenMP build compiles the maxima out (both stay 0); with
+         * dt_dynamic_reduce they are the serial build's max |a_j| and max arvmu_j. */
+        if (p->dt_correction_method == 2) {
+            double amax = 0, mumax = 0;
+            if (p->dt_dynamic_reduce) {
+                for (uint64_t j = 0; j < n; j++) {
+                    const double* aj = a + j * stride;
+                    double l2 = aj[0] * aj[0] + aj[1] * aj[1];
+                    if (dim == 3) l2 += aj[2] * aj[2];
+                    const double am = sqrt(l2);
+                    if (am > amax) amax = am;
+                    if (mu[j] > mumax) mumax = mu[j];
+                }
+            }
+            const double c0 = orc_eos_c(p);
+            const double min_dt_a = sqrt(p->hsml / amax);
+            const double min_dt_mu = p->hsml / (c0 + mumax);
+            p->dt = p->CFL_coef * (min_dt_mu < min_dt_a ? min_dt_mu : min_dt_a);
+            if (p->dt <= (p->hsml / c0) * 1.E-6) { rc = RRSPH_ERR_NEVER_ENDING; goto done; }
+        }
         /* piston */
         if (p->nwm && time >= p->nwm_time_start) orc_make_waves(p, r, v, stride, itype, time);
         /* whole_step */
@@ -711,7 +733,7 @@ int orc_run(rrsph_params* p, double* r, double* v, uint32_t stride, double* rho,
     }
 done:
     *time_io = time;
-    free(v_pred); free(rho_pred); free(av); free(keys); free(grid); free(cells);
+    free(v_pred); free(rho_pred); free(av); free(mu); free(keys); free(grid); free(cells);
     free(counts); free(list);
     return rc;
 }

@@ -103,6 +103,19 @@ double orc_gauge(const rrsph_params* p, const double* r, uint32_t stride,
                  const int32_t* itype, double x_gauge, double search_n,
                  int32_t type_filter);
 
+/* Forward run of the loop with a Fourier piston, X(t) = sum_k coef[k-1]
+ * sin(k omega t) on the nwm particle range, and its forward-mode derivatives
+ * (rrsph_tangent.c). Gauges of the states after sample_from, sample_from +
+ * sample_every, ... <= nsteps steps go to gauges[s]; their derivatives by the
+ * coefficients to dgauges[s * ncoef + k]. Method set: 2D, summation density,
+ * cubic kernel, no artificial pressure / XSPH, constant dt, nwm == 2; otherwise
+ * RRSPH_ERR_UNSUPPORTED. */
+int orc_piston_tangent_run(rrsph_params* p, double* r, double* v, uint32_t stride, double* rho, double* pres,
+                           int32_t* itype, double* a, uint64_t nsteps, double* time_io, uint32_t ncoef,
+                           double omega, const double* coef, double gauge_x, double search_n, int32_t gauge_type,
+                           uint64_t sample_from, uint64_t sample_every, double* gauges, double* dgauges,
+                           uint64_t max_samples, uint64_t* nsamples);
+
 /* Threads the oracle uses (OpenMP); <= 0 keeps the runtime default. */
 void orc_set_threads(int n);
 int orc_get_threads(void);

@@ -33,7 +33,7 @@ REF_BIN = ORACLE_DIR / "_ref" / "rrsph_ref"
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CU_SOURCES = ["sort.cu", "kernels_common.cu", "kernels_fp64.cu", "kernels_mixed.cu", "solver.cu", "sort_noalloc.cu",
-              "run_loop.cu"]
+              "run_loop.cu", "adjoint.cu"]
 CPP_SOURCES = ["params.cpp", "layers.cpp"]
 
 
@@ -109,12 +109,12 @@ def build_cuda(verbose: bool = False, extra_nvcc=()) -> Path:
 
 def build_oracle(verbose: bool = False) -> Path:
     """Compiles the C oracle into ``oracle/liboracle.so``."""
-    src = ORACLE_DIR / "rrsph_oracle.c"
+    srcs = [ORACLE_DIR / "rrsph_oracle.c", ORACLE_DIR / "rrsph_tangent.c"]
     hdrs = [ORACLE_DIR / "rrsph_oracle.h", ROOT / "include" / "rrsph_cuda.h"]
-    if not _newer(ORACLE_LIB, [src, *hdrs]):
+    if not _newer(ORACLE_LIB, [*srcs, *hdrs]):
         tmp = ORACLE_LIB.with_suffix(".so.tmp")
         _run(["gcc", "-std=c11", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-Wall", "-o", tmp,
-              src, "-lm"], verbose)
+              *srcs, "-lm"], verbose)
         os.replace(tmp, ORACLE_LIB)
     return ORACLE_LIB
 

@@ -99,6 +99,24 @@ class RrsphParams(C.Structure):
         return out
 
 
+PISTON_FOURIER_MAX = 16
+
+
+class RrsphAdjointConfig(C.Structure):
+    """Mirror of rrsph_adjoint_config."""
+
+    _fields_ = [
+        ("struct_size", C.c_uint32),
+        ("checkpoint_every", C.c_uint32),
+        ("nsteps", C.c_uint64),
+        ("gauge_x", C.c_double),
+        ("gauge_search_n", C.c_double),
+        ("gauge_type", C.c_int32),
+        ("sample_every", C.c_uint32),
+        ("sample_from", C.c_uint64),
+    ]
+
+
 _lib = None
 
 _P = C.POINTER
@@ -141,6 +159,9 @@ _SIGS = {
     "rrsph_kernel_launches": (C.c_int, [C.c_void_p, _P(C.c_uint64)]),
     "rrsph_sort_pairs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
                                            C.c_void_p]),
+    "rrsph_set_piston_fourier": (C.c_int, [C.c_void_p, C.c_uint32, C.c_double, _dp]),
+    "rrsph_adjoint_forward": (C.c_int, [C.c_void_p, _P(RrsphAdjointConfig), _dp, _dp, C.c_uint64, _P(C.c_uint64)]),
+    "rrsph_adjoint_reverse": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
 }
 
 

@@ -221,6 +221,36 @@ def piston_flume_2d(seed: int = 7, nx: int = 4000, ny: int = 100, dx: float = 0.
                        "piston_amplitude": amplitude, "gauges_x": [2.0, 5.0, 10.0]})
 
 
+def fourier_coefficients(seed: int, n: int = 8, lo: float = 0.005, hi: float = 0.03) -> np.ndarray:
+    """Seeded amplitudes of the Fourier piston X(t) = sum_k c_k sin(k omega t)."""
+    return np.random.default_rng(seed).uniform(lo, hi, size=n)
+
+
+def adjoint_flume_2d(seed: int = 7, nx: int = 2000, ny: int = 100, dx: float = 0.005, coef_seed: int = 2,
+                     target_seed: int = 3, ncoef: int = 8, period: float = 8.0, steps: int = 5000,
+                     gauge_x: float = 0.3, window: float = 0.1, sample_every: int = 10) -> Case:
+    """Piston flume for the adjoint: nx x ny fluid lattice (2000 x 100 =
+    200,000 at dx = 0.005: 10 m x 0.5 m), the piston moving as the Fourier
+    series X(t) = sum_k c_k sin(k omega t), omega = 2 pi / period, with c from
+    ``coef_seed`` (amplitudes 0.005-0.03 m) and the target series from
+    ``target_seed``. The loss is the mean squared gauge misfit at gauge_x over
+    the last ``window`` seconds of ``steps`` steps, sampled every
+    ``sample_every`` steps (5,000 steps are 0.22 s, so the gauge sits 0.3 m
+    from the piston)."""
+    case = piston_flume_2d(seed=seed, nx=nx, ny=ny, dx=dx, steps=steps)
+    dt = case.notes["dt"]
+    sample_from = max(0, steps - int(round(window / dt)))
+    sample_from += (steps - sample_from) % sample_every  # the last sample is the last state
+    case.name = "adjoint_flume_2d"
+    case.notes.update({
+        "omega": 2.0 * math.pi / period, "coef": fourier_coefficients(coef_seed, ncoef),
+        "target_coef": fourier_coefficients(target_seed, ncoef), "coef_seed": coef_seed, "target_seed": target_seed,
+        "piston_period": period, "gauge_x": gauge_x, "sample_from": sample_from, "sample_every": sample_every,
+        "window": window,
+    })
+    return case
+
+
 def dam_break_3d(seed: int = 3, dx: float = 0.0026, tank=(1.6, 0.67, 0.6), block=(0.4, 0.67, 0.3),
                  steps: int = 5000, density_treatment: int = 1, max_neighbours: int = 400) -> Case:
     """3D dam break: fluid block inside a tank with LJ floor and walls at dx/2,

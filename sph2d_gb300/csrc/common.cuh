@@ -64,6 +64,10 @@ struct DevParams {
     uint32_t nwm_start, nwm_end;
     int nwm_valid;
     double nwm_time_start, nwm_phase, nwm_freq, nwm_H, nwm_k, depth;
+    // Fourier piston (rrsph_set_piston_fourier): X(t) = sum_k fourier_coef[k-1] sin(k omega t)
+    int fourier_n;          // 0: the wave maker's own law
+    double fourier_omega;
+    double fourier_coef[16];
     // dt control
     int dt_method;          // 0 const, 1 CFL const, 2 dynamic
     int dt_reduce;          // 1: true max reduction

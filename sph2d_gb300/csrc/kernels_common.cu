@@ -109,8 +109,17 @@ __global__ void k_reorder(DevParams P, State S, Sorted G, GatherSrc F, int mixed
     }
 }
 
-// Piston velocity of dynamic_boundaries (RRSPH_OMP/src/WaveMaker.cpp:34-82).
+// Piston velocity of dynamic_boundaries (RRSPH_OMP/src/WaveMaker.cpp:34-82),
+// or X'(t) of the Fourier piston X(t) = sum_k c_k sin(k omega t) when one is set.
 __device__ double piston_vx(const DevParams& P, double time) {
+    if (P.fourier_n > 0) {
+        double vx = 0;
+        for (int k = 1; k <= P.fourier_n; k++) {
+            const double phi = k * P.fourier_omega * cos(k * P.fourier_omega * time);
+            vx += P.fourier_coef[k - 1] * phi;
+        }
+        return vx;
+    }
     const double delta = P.nwm_phase - P.nwm_freq * P.nwm_time_start;
     const double omega = P.nwm_freq;
     const double H = P.nwm_H;

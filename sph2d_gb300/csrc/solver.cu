@@ -276,6 +276,8 @@ int flags_to_status(const rrsph_solver* s, uint32_t f) {
 
 }  // namespace
 
+int rrsph_impl::flags_status(const rrsph_solver* s, uint32_t f) { return flags_to_status(s, f); }
+
 // ============================================================== C ABI ======
 
 extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver** out) {
@@ -360,6 +362,7 @@ extern "C" void rrsph_destroy(rrsph_solver* s) {
     if (!s) return;
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
+    rrsph_impl::adjoint_release(s);
     for (int i = 0; i < 2; i++)
         if (s->graph[i]) cudaGraphExecDestroy(s->graph[i]);
     for (int i = 0; i <= kPhases; i++)

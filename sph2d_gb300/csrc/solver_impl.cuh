@@ -11,6 +11,8 @@ constexpr int kPhases = 6;
 inline const char* const kPhaseNames[kPhases] = {"keys", "sort", "reorder", "density", "forces", "whole"};
 constexpr uint32_t kFlagNeverEnding = RRSPH_FLAG_NEVER_ENDING;
 
+struct AdjointRun;  // a forward run recorded for the reverse sweep (adjoint.cu)
+
 }  // namespace rrsph_impl
 
 using rrsph_impl::kPhases;
@@ -45,5 +47,13 @@ struct rrsph_solver {
     cudaEvent_t ev[kPhases + 1] = {};
     double phase_ms[kPhases] = {};
     uint64_t timed_steps = 0;
+    rrsph_impl::AdjointRun* adj = nullptr;
 };
+
+namespace rrsph_impl {
+// Frees the recorded adjoint run of s, if any (adjoint.cu).
+void adjoint_release(rrsph_solver* s);
+// The status (and error message) the device flags f mean for s (solver.cu).
+int flags_status(const rrsph_solver* s, uint32_t f);
+}  // namespace rrsph_impl
 

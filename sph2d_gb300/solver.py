@@ -211,6 +211,36 @@ class Solver:
         check(lib().rrsph_forces(self._h, terms, _dp(a), self.dim, _dp(av), _dp(mu)))
         return a, av, mu
 
+    # -- piston optimisation
+    def set_piston_fourier(self, omega: float, coef) -> None:
+        """Piston displacement X(t) = sum_k coef[k-1] sin(k omega t) (empty coef: the wave maker's own law)."""
+        c = np.ascontiguousarray(coef, dtype=np.float64)
+        self._fourier_n = int(c.size)
+        check(lib().rrsph_set_piston_fourier(self._h, c.size, float(omega), _dp(c) if c.size else None))
+
+    def adjoint_forward(self, nsteps: int, gauge_x: float, sample_from: int = 0, sample_every: int = 1,
+                        checkpoint_every: int = 100, search_n: float = 3.0, gauge_type: int = 2,
+                        time: float = 0.0):
+        """Recorded FP64 forward run; returns (gauge series, time at the end)."""
+        cfg = capi.RrsphAdjointConfig(C.sizeof(capi.RrsphAdjointConfig), checkpoint_every, nsteps, gauge_x, search_n,
+                                      gauge_type, sample_every, sample_from)
+        cap = (nsteps - sample_from) // sample_every + 1 if nsteps >= sample_from else 0
+        g = np.zeros(max(cap, 1))
+        t = C.c_double(time)
+        ns = C.c_uint64()
+        self._adj_steps = 0
+        check(lib().rrsph_adjoint_forward(self._h, C.byref(cfg), C.byref(t), _dp(g), cap, C.byref(ns)))
+        self._adj_steps = nsteps
+        return g[: int(ns.value)], t.value
+
+    def adjoint_reverse(self, dgauges):
+        """(dL/dcoef of the Fourier piston, dL/d(piston vx) per step) for dL/dgauge."""
+        dg = np.ascontiguousarray(dgauges, dtype=np.float64)
+        dcoef = np.zeros(max(getattr(self, "_fourier_n", 0), 1))
+        dvx = np.zeros(max(getattr(self, "_adj_steps", 0), 1))
+        check(lib().rrsph_adjoint_reverse(self._h, _dp(dg), _dp(dcoef), _dp(dvx)))
+        return dcoef[: getattr(self, "_fourier_n", 0)], dvx[: self._adj_steps]
+
     # -- timing
     def phase_names(self) -> list[str]:
         c = C.c_int()

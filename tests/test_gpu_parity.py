@@ -391,6 +391,29 @@ def test_dynamic_dt_follows_the_omp_build(gpu_available):
     assert t == pytest.approx(5 * dt, rel=1e-12)
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("mixed", 1e-4)])
+def test_dynamic_dt_with_the_true_maxima(gpu_available, precision, tol):
+    """dt_dynamic_reduce: dt from the device max of |a_j| and arvmu_j each step
+    (UpdateAcceleration.cpp:15-29, the serial build's reduction), against the
+    oracle's; the time after 12 steps sums 12 different dts."""
+    from oracle import binding as O
+    from sph2d_gb300 import Solver
+
+    case = _dam(nx=30, ny=15)
+    p = case.params()
+    p.dt_correction_method = 2
+    p.dt_dynamic_reduce = 1
+    p.CFL_coef = 0.2
+    ref = O.run(p, case.r, case.v, case.rho, case.itype, nsteps=12)
+    with Solver(p, precision) as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        t = s.step(12, 0.0)
+        st = s.download()
+    assert t == pytest.approx(ref["time"], rel=tol)
+    for k in ("r", "v", "rho"):
+        assert rel_l2(st[k], ref[k]) < tol, k
+
+
 def test_graph_replay_equals_direct_launches(gpu_available):
     from sph2d_gb300 import Solver
 
