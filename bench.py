@@ -315,11 +315,123 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         "gpu_launches": launches,
         "clocks": clocks_info,
     }
+    sm.close()
+    s64.close()
+    if rank == 0 and world == 1 and not args.no_ensemble:
+        result["ensemble"] = ensemble_measure()
+    if rank == 0 and world == 1 and not args.no_adjoint:
+        result["adjoint"] = adjoint_measure(steps=args.adjoint_steps)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(case, p, steps=args.cpu_steps)
     if dist:
         dist.destroy_process_group()
     return result
+
+
+def ensemble_measure(steps: int = 50, seq_steps: int = 10, ntanks: int = 256) -> dict:
+    """Batched ensemble: every tank packed into one mixed-precision solver (one
+    graph launch per step for all tanks, gather block sizes from the
+    autotuner) against the same tanks stepped one after another, each in its
+    own solver."""
+    import torch
+
+    from sph2d_gb300 import Solver, cases
+
+    tanks = cases.ensemble_tanks(ntanks=ntanks)
+    ens = cases.pack_tanks(tanks)
+    p = ens.params()
+    with Solver(p, "mixed") as s:
+        s.upload(ens.r, ens.v, ens.rho, ens.itype)
+        s.set_wave_makers(ens.notes["wave_makers"])
+        s.set_time(0.0)
+        s.step_async(3)
+        s.sync()
+        threads = s.autotune(steps=3)
+        s.step_async(3)
+        s.sync()
+        _, q0 = s.pair_count()
+        ext = torch.cuda.ExternalStream(s.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        s.step_async(steps)
+        e1.record(ext)
+        s.sync()
+        ms = e0.elapsed_time(e1)
+        _, q1 = s.pair_count()
+        launches = s.kernel_launches()
+    seq_ms = 0.0
+    seq_pairs = 0
+    for c in tanks:
+        with Solver(c.params(), "mixed") as s:
+            s.upload(c.r, c.v, c.rho, c.itype)
+            s.set_wave_makers([c.notes["wave_maker"]])
+            s.set_time(0.0)
+            s.step_async(5)
+            s.sync()
+            _, a0 = s.pair_count()
+            ext = torch.cuda.ExternalStream(s.stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            s.step_async(seq_steps)
+            e1.record(ext)
+            s.sync()
+            seq_ms += e0.elapsed_time(e1) / seq_steps
+            _, a1 = s.pair_count()
+            seq_pairs += (a1 - a0) / seq_steps
+    batched_rate = (q1 - q0) / (ms / 1e3)
+    seq_rate = seq_pairs / (seq_ms / 1e3)
+    return {
+        "workload": f"{ntanks} independent 2D piston tanks, fluid counts log-uniform 2,000-60,000 (seed 4), depths "
+                    "0.2-0.6 m, length = count dx^2 / depth, dx 0.005 m, own piston amplitude 0.01-0.05 m and "
+                    "period 1-2 s (seed 5); FP32-mixed step",
+        "tanks": ntanks, "particles": ens.ntotal, "fluid_particles": int(ens.notes["nfluid"]),
+        "batched": {"ms_per_step": ms / steps, "pair_interactions_per_s": batched_rate, "steps": steps,
+                    "gather_threads": {"density": threads[0], "forces": threads[1]}},
+        "sequential": {"ms_per_step": seq_ms, "pair_interactions_per_s": seq_rate, "steps_per_tank": seq_steps},
+        "speedup": seq_ms / (ms / steps),
+        "launches_in_batched_region": launches,
+    }
+
+
+def adjoint_measure(steps: int = 500, checkpoint_every: int = 100) -> dict:
+    """Cost of d(gauge misfit)/d(piston Fourier coefficients) against a
+    forward run: the 2D adjoint flume (2000 x 100 fluid at dx 0.005 m, 8
+    Fourier coefficients), FP64."""
+    import torch
+
+    from sph2d_gb300 import Solver, cases
+
+    case = cases.adjoint_flume_2d(steps=steps)
+    p = case.params()
+    om, coef = case.notes["omega"], case.notes["coef"]
+    sf, se = case.notes["sample_from"], case.notes["sample_every"]
+    with Solver(p, "fp64") as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        s.set_piston_fourier(om, case.notes["target_coef"])
+        target, _ = s.adjoint_forward(steps, case.notes["gauge_x"], sf, se, checkpoint_every)
+        s.upload(case.r, case.v, case.rho, case.itype)
+        s.set_piston_fourier(om, coef)
+        s.step(5, 0.0)
+        s.upload(case.r, case.v, case.rho, case.itype)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.step(steps, 0.0)
+        fwd = time.perf_counter() - t0
+        s.upload(case.r, case.v, case.rho, case.itype)
+        t0 = time.perf_counter()
+        g, _ = s.adjoint_forward(steps, case.notes["gauge_x"], sf, se, checkpoint_every)
+        t1 = time.perf_counter()
+        dcoef, _ = s.adjoint_reverse(2.0 * (g - target) / len(g))
+        t2 = time.perf_counter()
+    return {
+        "workload": f"2D adjoint flume, {case.ntotal} particles (2000 x 100 fluid, 10 m x 0.5 m at dx 0.005 m), "
+                    f"8 Fourier piston coefficients (seed 2, target seed 3), gauge x = {case.notes['gauge_x']} m, "
+                    f"{len(g)} samples every {se} steps over the last {case.notes['window']} s; {steps} steps, "
+                    f"checkpoints every {checkpoint_every}",
+        "forward_s": fwd, "adjoint_forward_s": t1 - t0, "adjoint_reverse_s": t2 - t1,
+        "gradient_cost_vs_forward": (t2 - t0) / fwd,
+        "loss": float(np.mean((g - target) ** 2)), "dloss_dcoef": [float(x) for x in dcoef],
+    }
 
 
 def _profile_traffic():
@@ -412,6 +524,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the 256-tank ensemble measurement")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost measurement")
+    ap.add_argument("--adjoint-steps", type=int, default=500)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         ap.error("--warmup must be >= 3")

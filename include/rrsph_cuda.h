@@ -337,6 +337,29 @@ int rrsph_adjoint_forward(rrsph_solver* s, const rrsph_adjoint_config* cfg, doub
  * state at the end of the forward run. */
 int rrsph_adjoint_reverse(rrsph_solver* s, const double* dgauges, double* dcoef, double* dpiston_vx);
 
+/* ---- ensembles of tanks and tuning ---------------------------------------- */
+/* One piston of an ensemble: the particles [particles_start, particles_end)
+ * move with dynamic_boundaries' law (WaveMaker.cpp:34-82) built from these
+ * parameters, as the params' nwm_* fields build it for a single experiment
+ * (wave number 2 pi / wave_length, frequency sqrt(g k tanh(k depth)),
+ * Input.cpp:125-137). */
+typedef struct rrsph_wave_maker {
+    uint64_t particles_start, particles_end;
+    uint32_t nwm;            /* 2: first order, 3: second order */
+    uint32_t reserved;
+    double time_start, phase, wave_length, wave_magnitude, depth;
+} rrsph_wave_maker;
+/* Replaces the params' wave maker by a table of pistons, one per tank of an
+ * ensemble packed into one particle set (count = 0 restores the params' wave
+ * maker). Ranges must not overlap. */
+int rrsph_set_wave_makers(rrsph_solver* s, uint32_t count, const rrsph_wave_maker* makers);
+/* Block sizes of the density and force gathers (multiples of 32, <= 256). */
+int rrsph_set_gather_threads(rrsph_solver* s, uint32_t density_threads, uint32_t force_threads);
+/* Autotuner: times `steps` steps on the uploaded state for every pair of
+ * candidate gather block sizes (64, 128, 256), keeps the fastest and puts the
+ * state back. threads_out[2] (may be NULL) receives {density, forces}. */
+int rrsph_autotune(rrsph_solver* s, uint32_t steps, uint32_t* threads_out);
+
 /* ---- timing hooks for benchmarks ------------------------------------------ */
 /* Number of kernel phases one step launches and their names. */
 int rrsph_phase_count(rrsph_solver* s, int* count);

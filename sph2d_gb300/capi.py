@@ -117,6 +117,22 @@ class RrsphAdjointConfig(C.Structure):
     ]
 
 
+class RrsphWaveMaker(C.Structure):
+    """Mirror of rrsph_wave_maker."""
+
+    _fields_ = [
+        ("particles_start", C.c_uint64),
+        ("particles_end", C.c_uint64),
+        ("nwm", C.c_uint32),
+        ("reserved", C.c_uint32),
+        ("time_start", C.c_double),
+        ("phase", C.c_double),
+        ("wave_length", C.c_double),
+        ("wave_magnitude", C.c_double),
+        ("depth", C.c_double),
+    ]
+
+
 _lib = None
 
 _P = C.POINTER
@@ -162,6 +178,9 @@ _SIGS = {
     "rrsph_set_piston_fourier": (C.c_int, [C.c_void_p, C.c_uint32, C.c_double, _dp]),
     "rrsph_adjoint_forward": (C.c_int, [C.c_void_p, _P(RrsphAdjointConfig), _dp, _dp, C.c_uint64, _P(C.c_uint64)]),
     "rrsph_adjoint_reverse": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
+    "rrsph_set_wave_makers": (C.c_int, [C.c_void_p, C.c_uint32, _P(RrsphWaveMaker)]),
+    "rrsph_set_gather_threads": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
+    "rrsph_autotune": (C.c_int, [C.c_void_p, C.c_uint32, _u32p]),
 }
 
 

@@ -251,6 +251,88 @@ def adjoint_flume_2d(seed: int = 7, nx: int = 2000, ny: int = 100, dx: float = 0
     return case
 
 
+def ensemble_tanks(ntanks: int = 256, seed: int = 4, wave_seed: int = 5, n_lo: int = 2000, n_hi: int = 60000,
+                   depth_lo: float = 0.2, depth_hi: float = 0.6, dx: float = 0.005, amp_lo: float = 0.01,
+                   amp_hi: float = 0.05, period_lo: float = 1.0, period_hi: float = 2.0,
+                   steps: int = 2000) -> list[Case]:
+    """Independent 2D piston tanks: fluid counts log-uniform in [n_lo, n_hi]
+    and depths uniform in [depth_lo, depth_hi] (seed), length = count dx^2 /
+    depth; each piston with its own amplitude and period (wave_seed). Every
+    tank shares c0, h and dt (the flume's); its piston law uses its own depth.
+    Each case carries notes["wave_maker"] for rrsph_set_wave_makers."""
+    rng = np.random.default_rng(seed)
+    wrng = np.random.default_rng(wave_seed)
+    counts = np.exp(rng.uniform(math.log(n_lo), math.log(n_hi), ntanks))
+    depths = rng.uniform(depth_lo, depth_hi, ntanks)
+    amps = wrng.uniform(amp_lo, amp_hi, ntanks)
+    periods = wrng.uniform(period_lo, period_hi, ntanks)
+    out = []
+    for t in range(ntanks):
+        ny = max(4, int(round(depths[t] / dx)))
+        nx = max(4, int(round(counts[t] / ny)))
+        c = piston_flume_2d(seed=seed * 100003 + t, nx=nx, ny=ny, dx=dx, tank_height=ny * dx + 0.3, steps=steps)
+        d = ny * dx
+        k = piston_wave_number(periods[t], d)
+        kd = k * d
+        m1 = 2 * math.sinh(kd) ** 2 / (math.sinh(kd) * math.cosh(kd) + kd)
+        c.name = f"tank{t}"
+        c.notes.update({"amplitude": float(amps[t]), "period": float(periods[t]), "water_depth": d})
+        c.notes["wave_maker"] = {
+            "particles_start": int(c.particle["nwm_particles_start"]),
+            "particles_end": int(c.particle["nwm_particles_end"]),
+            "nwm": 2, "time_start": 0.0, "phase": 0.0, "wave_length": 2.0 * math.pi / k,
+            "wave_magnitude": 2.0 * float(amps[t]) * m1, "depth": d,
+        }
+        out.append(c)
+    return out
+
+
+def pack_tanks(tanks: list[Case], gap: float = 0.3) -> Case:
+    """One particle set holding every tank, laid out in rows on a square-ish
+    plane with `gap` between tanks (far beyond the 2h interaction range), for
+    one solver over the whole ensemble. notes["wave_makers"] lists the pistons
+    with global particle ranges; notes["offsets"] the (x, y) shift of each tank
+    and notes["ranges"] its particle range."""
+    foot = [(c.notes["tank_length"] + 2 * gap, c.particle["y_maxgeom"] - c.particle["y_mingeom"] + gap)
+            for c in tanks]
+    width = math.sqrt(sum(w * h for w, h in foot) * 1.3)
+    offsets, x, y, row_h = [], 0.0, 0.0, 0.0
+    for w, h in foot:
+        if x > 0 and x + w > width:
+            x, y, row_h = 0.0, y + row_h, 0.0
+        offsets.append((x + gap, y))
+        x += w
+        row_h = max(row_h, h)
+    rs, vs, rhos, its, makers, ranges = [], [], [], [], [], []
+    base = 0
+    for c, (ox, oy) in zip(tanks, offsets):
+        rs.append(c.r + np.array([ox, oy]))
+        vs.append(c.v)
+        rhos.append(c.rho)
+        its.append(c.itype)
+        m = dict(c.notes["wave_maker"])
+        m["particles_start"] += base
+        m["particles_end"] += base
+        makers.append(m)
+        ranges.append((base, base + c.ntotal))
+        base += c.ntotal
+    r = np.concatenate(rs)
+    model = dict(tanks[0].model)
+    model["nwm"] = 0
+    particle = dict(tanks[0].particle)
+    particle.update({
+        "x_mingeom": float(r[:, 0].min()) - 0.5, "x_maxgeom": float(r[:, 0].max()) + 0.5,
+        "y_mingeom": float(r[:, 1].min()) - 0.1, "y_maxgeom": float(r[:, 1].max()) + 0.5,
+        "ntotal": int(base), "nfluid": int(sum(c.notes["nfluid"] for c in tanks)),
+        "nvirt": int(sum(c.notes["nboundary"] for c in tanks)),
+        "nwm_particles_start": 0, "nwm_particles_end": 0,
+    })
+    return Case("ensemble_2d", model, particle, r, np.concatenate(vs), np.concatenate(rhos),
+                np.concatenate(its).astype(np.int32),
+                notes={"tanks": len(tanks), "wave_makers": makers, "offsets": offsets, "ranges": ranges,
+                       "dt": tanks[0].notes["dt"], "nfluid": particle["nfluid"]})
+
+
 def dam_break_3d(seed: int = 3, dx: float = 0.0026, tank=(1.6, 0.67, 0.6), block=(0.4, 0.67, 0.3),
                  steps: int = 5000, density_treatment: int = 1, max_neighbours: int = 400) -> Case:
     """3D dam break: fluid block inside a tank with LJ floor and walls at dx/2,

@@ -76,6 +76,13 @@ struct DevParams {
     MixedF mf;
 };
 
+// One piston of a wave-maker table (rrsph_set_wave_makers): the law of
+// dynamic_boundaries (WaveMaker.cpp:34-82) with its own parameters.
+struct PistonLaw {
+    int nwm;  // 2: first order, 3: second order
+    double time_start, phase, freq, H, k, depth;
+};
+
 // Per-step scalars kept on the device (double-buffered by step parity so a
 // captured step graph can advance them without host involvement).
 struct StepScalars {

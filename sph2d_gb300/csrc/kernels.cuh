@@ -19,6 +19,8 @@ struct State {
     double *mu;                // max |mu_ij| per particle (rrsph_forces only)
     int32_t* itype;
     uint32_t* key_of;          // cell key used by the last grid build, per id
+    int32_t* wave_tank;        // piston of each particle in wave_law, -1 for none (null: the params' wave maker)
+    const PistonLaw* wave_law; // wave-maker table
 };
 
 // Per-step cell-ordered copies and the grid.
@@ -60,18 +62,20 @@ void launch_keys(const DevParams& P, const State& S, Sorted& G, StepScalars* sca
                  cudaStream_t st);
 template <int DIM>
 void launch_reorder(const DevParams& P, const State& S, const Sorted& G, GatherSrc fsrc, int mixed, cudaStream_t st);
+// The pair gathers take their block size (threads, <= kMaxGatherThreads, a
+// multiple of 32) from the caller; the autotuner picks it.
 template <int DIM>
 void launch_density_fp64(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
-                         cudaStream_t st);
+                         cudaStream_t st, int threads);
 template <int DIM>
 void launch_forces_fp64(const DevParams& P, const State& S, const Sorted& G, uint32_t terms, StepScalars* scal,
-                        uint32_t* flags, int write_mu, cudaStream_t st);
+                        uint32_t* flags, int write_mu, cudaStream_t st, int threads);
 template <int DIM>
 void launch_density_mixed(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
-                          cudaStream_t st);
+                          cudaStream_t st, int threads);
 template <int DIM>
 void launch_forces_mixed(const DevParams& P, const State& S, const Sorted& G, uint32_t terms, StepScalars* scal,
-                         uint32_t* flags, int write_mu, int use_masks, cudaStream_t st);
+                         uint32_t* flags, int write_mu, int use_masks, cudaStream_t st, int threads);
 // whole_step; with next_keys also the next step's predict_half_step and key pass.
 template <int DIM>
 void launch_whole_step(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal_cur,
@@ -86,6 +90,7 @@ void launch_unpack(const DevParams& P, State S, const double* r, const double* v
 template <int DIM>
 void launch_pack(const DevParams& P, State S, double* r, double* v, uint32_t stride, cudaStream_t st);
 
-constexpr int kGatherThreads = 128;
+constexpr int kGatherThreads = 128;     // default block size of the pair gathers
+constexpr int kMaxGatherThreads = 256;
 
 }  // namespace rrsph

@@ -109,8 +109,27 @@ __global__ void k_reorder(DevParams P, State S, Sorted G, GatherSrc F, int mixed
     }
 }
 
-// Piston velocity of dynamic_boundaries (RRSPH_OMP/src/WaveMaker.cpp:34-82),
-// or X'(t) of the Fourier piston X(t) = sum_k c_k sin(k omega t) when one is set.
+// Piston velocity of dynamic_boundaries (RRSPH_OMP/src/WaveMaker.cpp:34-82)
+// for one set of wave-maker parameters.
+__device__ double piston_law_vx(int nwm, double phase, double freq, double H, double k, double depth,
+                                double time_start, double time) {
+    const double delta = phase - freq * time_start;
+    const double omega = freq;
+    const double kd = k * depth;
+    const double sh = sinh(kd), ch = cosh(kd);
+    const double m1 = 2 * (sh * sh) / (sh * ch + kd);
+    const double S0 = H / m1;
+    double vx = 0.5 * S0 * omega * cos(omega * time + delta);
+    if (nwm == 3) {
+        const double e2_1 = (H * H) / (32 * depth);
+        const double e2_2 = 3 * ch / (sh * sh * sh) - 2 / m1;
+        vx += 2 * omega * (e2_1 + e2_2) * cos(2 * omega * time + 2 * delta);
+    }
+    return vx;
+}
+
+// The params' piston, or X'(t) of the Fourier piston X(t) = sum_k c_k
+// sin(k omega t) when one is set.
 __device__ double piston_vx(const DevParams& P, double time) {
     if (P.fourier_n > 0) {
         double vx = 0;
@@ -120,20 +139,7 @@ __device__ double piston_vx(const DevParams& P, double time) {
         }
         return vx;
     }
-    const double delta = P.nwm_phase - P.nwm_freq * P.nwm_time_start;
-    const double omega = P.nwm_freq;
-    const double H = P.nwm_H;
-    const double kd = P.nwm_k * P.depth;
-    const double sh = sinh(kd), ch = cosh(kd);
-    const double m1 = 2 * (sh * sh) / (sh * ch + kd);
-    const double S0 = H / m1;
-    double vx = 0.5 * S0 * omega * cos(omega * time + delta);
-    if (P.nwm == 3) {
-        const double e2_1 = (H * H) / (32 * P.depth);
-        const double e2_2 = 3 * ch / (sh * sh * sh) - 2 / m1;
-        vx += 2 * omega * (e2_1 + e2_2) * cos(2 * omega * time + 2 * delta);
-    }
-    return vx;
+    return piston_law_vx(P.nwm, P.nwm_phase, P.nwm_freq, P.nwm_H, P.nwm_k, P.depth, P.nwm_time_start, time);
 }
 
 // Piston velocity of nwm_solitary_rayleigh (WaveMaker.cpp:84-134).
@@ -183,7 +189,17 @@ __global__ void k_whole(DevParams P, State S, Sorted G, const StepScalars* __res
     }
     if (i >= P.n) return;
     const bool waves = P.nwm && !nwm_off && time >= P.nwm_time_start;
-    if (waves && P.nwm_valid && i >= P.nwm_start && i < P.nwm_end) {
+    if (S.wave_tank) {  // a table of pistons (one per tank of an ensemble)
+        const int32_t w = S.wave_tank[i];
+        if (w >= 0) {
+            const PistonLaw L = S.wave_law[w];
+            if (time >= L.time_start) {
+                const double vx = piston_law_vx(L.nwm, L.phase, L.freq, L.H, L.k, L.depth, L.time_start, time);
+                S.rx[i] = S.rx[i] + vx * dt;
+                S.vx[i] = vx;
+            }
+        }
+    } else if (waves && P.nwm_valid && i >= P.nwm_start && i < P.nwm_end) {
         if (P.nwm == 2 || P.nwm == 3 || P.nwm == 5) {
             const double vx = P.nwm == 5 ? solitary_vx(P, time) : piston_vx(P, time);
             S.rx[i] = S.rx[i] + vx * dt;

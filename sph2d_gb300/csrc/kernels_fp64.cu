@@ -25,7 +25,7 @@ __device__ __forceinline__ void warp_max_bits(unsigned long long* dst, double v)
 // density_sum (RRSPH_COMMON/include/Density.h:25-61) and density_con
 // (Density.h:63-114, delta-SPH when density_treatment == 2), EOS p (EOS.cpp:31-34).
 template <int DIM>
-__global__ void __launch_bounds__(kGatherThreads) k_density(DevParams P, State S, Sorted G,
+__global__ void __launch_bounds__(kMaxGatherThreads) k_density(DevParams P, State S, Sorted G,
                                                             StepScalars* __restrict__ scal,
                                                             uint32_t* __restrict__ flags) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_density(DevParams P, State S
 // (InternalForce.h:24-141), artificial_viscosity_part (ArtificialViscosity.h:29-65)
 // and average_velocity_part (AverageVelocity.h:20-37).
 template <int DIM>
-__global__ void __launch_bounds__(kGatherThreads) k_forces(DevParams P, State S, Sorted G, uint32_t terms,
+__global__ void __launch_bounds__(kMaxGatherThreads) k_forces(DevParams P, State S, Sorted G, uint32_t terms,
                                                            StepScalars* __restrict__ scal,
                                                            uint32_t* __restrict__ flags, int write_mu) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -223,23 +223,22 @@ __global__ void __launch_bounds__(kGatherThreads) k_forces(DevParams P, State S,
 
 template <int DIM>
 void launch_density_fp64(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
-                         cudaStream_t st) {
-    k_density<DIM><<<(P.n + kGatherThreads - 1) / kGatherThreads, kGatherThreads, 0, st>>>(P, S, G, scal, flags);
+                         cudaStream_t st, int threads) {
+    k_density<DIM><<<(P.n + threads - 1) / threads, threads, 0, st>>>(P, S, G, scal, flags);
 }
 template <int DIM>
 void launch_forces_fp64(const DevParams& P, const State& S, const Sorted& G, uint32_t terms, StepScalars* scal,
-                        uint32_t* flags, int write_mu, cudaStream_t st) {
-    k_forces<DIM><<<(P.n + kGatherThreads - 1) / kGatherThreads, kGatherThreads, 0, st>>>(P, S, G, terms, scal,
-                                                                                           flags, write_mu);
+                        uint32_t* flags, int write_mu, cudaStream_t st, int threads) {
+    k_forces<DIM><<<(P.n + threads - 1) / threads, threads, 0, st>>>(P, S, G, terms, scal, flags, write_mu);
 }
 
 template void launch_density_fp64<2>(const DevParams&, const State&, const Sorted&, StepScalars*, uint32_t*,
-                                     cudaStream_t);
+                                     cudaStream_t, int);
 template void launch_density_fp64<3>(const DevParams&, const State&, const Sorted&, StepScalars*, uint32_t*,
-                                     cudaStream_t);
+                                     cudaStream_t, int);
 template void launch_forces_fp64<2>(const DevParams&, const State&, const Sorted&, uint32_t, StepScalars*, uint32_t*,
-                                    int, cudaStream_t);
+                                    int, cudaStream_t, int);
 template void launch_forces_fp64<3>(const DevParams&, const State&, const Sorted&, uint32_t, StepScalars*, uint32_t*,
-                                    int, cudaStream_t);
+                                    int, cudaStream_t, int);
 
 }  // namespace rrsph

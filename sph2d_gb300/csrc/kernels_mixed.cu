@@ -108,7 +108,7 @@ __device__ __forceinline__ float eos_pf(const MixedF& M, float d) {
 // density_sum / density_con (Density.h:25-114) + EOS. SKF: 1 = cubic only
 // (every kernel choice cubic), 0 = any kernel (runtime switch).
 template <int DIM, int SKF>
-__global__ void __launch_bounds__(kGatherThreads) k_density_mixed(DevParams P, State S, Sorted G,
+__global__ void __launch_bounds__(kMaxGatherThreads) k_density_mixed(DevParams P, State S, Sorted G,
                                                                   StepScalars* __restrict__ scal,
                                                                   uint32_t* __restrict__ flags) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -298,7 +298,7 @@ struct ForceAcc {
 // MASKS: iterate the neighbour bits the density pass recorded (2D) instead of
 // searching the stencil cells again.
 template <int DIM, int SKF, bool MASKS>
-__global__ void __launch_bounds__(kGatherThreads) k_forces_mixed(DevParams P, State S, Sorted G, uint32_t terms,
+__global__ void __launch_bounds__(kMaxGatherThreads) k_forces_mixed(DevParams P, State S, Sorted G, uint32_t terms,
                                                                  StepScalars* __restrict__ scal,
                                                                  uint32_t* __restrict__ flags, int write_mu) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -450,32 +450,32 @@ __global__ void __launch_bounds__(kGatherThreads) k_forces_mixed(DevParams P, St
 
 template <int DIM>
 void launch_density_mixed(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
-                          cudaStream_t st) {
-    const unsigned blocks = (P.n + kGatherThreads - 1) / kGatherThreads;
-    if (P.all_cubic) k_density_mixed<DIM, 1><<<blocks, kGatherThreads, 0, st>>>(P, S, G, scal, flags);
-    else k_density_mixed<DIM, 0><<<blocks, kGatherThreads, 0, st>>>(P, S, G, scal, flags);
+                          cudaStream_t st, int threads) {
+    const unsigned blocks = (P.n + threads - 1) / threads;
+    if (P.all_cubic) k_density_mixed<DIM, 1><<<blocks, threads, 0, st>>>(P, S, G, scal, flags);
+    else k_density_mixed<DIM, 0><<<blocks, threads, 0, st>>>(P, S, G, scal, flags);
 }
 template <int DIM>
 void launch_forces_mixed(const DevParams& P, const State& S, const Sorted& G, uint32_t terms, StepScalars* scal,
-                         uint32_t* flags, int write_mu, int use_masks, cudaStream_t st) {
-    const unsigned blocks = (P.n + kGatherThreads - 1) / kGatherThreads;
+                         uint32_t* flags, int write_mu, int use_masks, cudaStream_t st, int threads) {
+    const unsigned blocks = (P.n + threads - 1) / threads;
     const bool m = DIM == 2 && use_masks && G.nbmask != nullptr;
     if (P.all_cubic) {
-        if (m) k_forces_mixed<DIM, 1, true><<<blocks, kGatherThreads, 0, st>>>(P, S, G, terms, scal, flags, write_mu);
-        else k_forces_mixed<DIM, 1, false><<<blocks, kGatherThreads, 0, st>>>(P, S, G, terms, scal, flags, write_mu);
+        if (m) k_forces_mixed<DIM, 1, true><<<blocks, threads, 0, st>>>(P, S, G, terms, scal, flags, write_mu);
+        else k_forces_mixed<DIM, 1, false><<<blocks, threads, 0, st>>>(P, S, G, terms, scal, flags, write_mu);
     } else {
-        if (m) k_forces_mixed<DIM, 0, true><<<blocks, kGatherThreads, 0, st>>>(P, S, G, terms, scal, flags, write_mu);
-        else k_forces_mixed<DIM, 0, false><<<blocks, kGatherThreads, 0, st>>>(P, S, G, terms, scal, flags, write_mu);
+        if (m) k_forces_mixed<DIM, 0, true><<<blocks, threads, 0, st>>>(P, S, G, terms, scal, flags, write_mu);
+        else k_forces_mixed<DIM, 0, false><<<blocks, threads, 0, st>>>(P, S, G, terms, scal, flags, write_mu);
     }
 }
 
 template void launch_density_mixed<2>(const DevParams&, const State&, const Sorted&, StepScalars*, uint32_t*,
-                                      cudaStream_t);
+                                      cudaStream_t, int);
 template void launch_density_mixed<3>(const DevParams&, const State&, const Sorted&, StepScalars*, uint32_t*,
-                                      cudaStream_t);
+                                      cudaStream_t, int);
 template void launch_forces_mixed<2>(const DevParams&, const State&, const Sorted&, uint32_t, StepScalars*, uint32_t*,
-                                     int, int, cudaStream_t);
+                                     int, int, cudaStream_t, int);
 template void launch_forces_mixed<3>(const DevParams&, const State&, const Sorted&, uint32_t, StepScalars*, uint32_t*,
-                                     int, int, cudaStream_t);
+                                     int, int, cudaStream_t, int);
 
 }  // namespace rrsph

@@ -12,6 +12,7 @@
 // The sequence is captured once per step parity into a CUDA graph and replayed;
 // the scalars that change between steps (time, dt, step counter) live on the
 // device, double-buffered by parity, and are advanced by the whole-step kernel.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -193,16 +194,18 @@ void enqueue_grid(rrsph_solver* s, int predict, rrsph::StepScalars* scal, rrsph:
 
 template <int DIM>
 void enqueue_density(rrsph_solver* s, rrsph::StepScalars* scal) {
-    if (s->precision == RRSPH_PRECISION_MIXED) rrsph::launch_density_mixed<DIM>(s->P, s->S, s->G, scal, s->flags, s->stream);
-    else rrsph::launch_density_fp64<DIM>(s->P, s->S, s->G, scal, s->flags, s->stream);
+    const int th = s->gather_threads[0];
+    if (s->precision == RRSPH_PRECISION_MIXED) rrsph::launch_density_mixed<DIM>(s->P, s->S, s->G, scal, s->flags, s->stream, th);
+    else rrsph::launch_density_fp64<DIM>(s->P, s->S, s->G, scal, s->flags, s->stream, th);
     s->launches++;
 }
 
 template <int DIM>
 void enqueue_forces(rrsph_solver* s, uint32_t terms, rrsph::StepScalars* scal, int write_mu, int use_masks = 0) {
+    const int th = s->gather_threads[1];
     if (s->precision == RRSPH_PRECISION_MIXED)
-        rrsph::launch_forces_mixed<DIM>(s->P, s->S, s->G, terms, scal, s->flags, write_mu, use_masks, s->stream);
-    else rrsph::launch_forces_fp64<DIM>(s->P, s->S, s->G, terms, scal, s->flags, write_mu, s->stream);
+        rrsph::launch_forces_mixed<DIM>(s->P, s->S, s->G, terms, scal, s->flags, write_mu, use_masks, s->stream, th);
+    else rrsph::launch_forces_fp64<DIM>(s->P, s->S, s->G, terms, scal, s->flags, write_mu, s->stream, th);
     s->launches++;
 }
 
@@ -711,5 +714,169 @@ extern "C" int rrsph_phase_times(rrsph_solver* s, double* ms_per_phase, int coun
 extern "C" int rrsph_kernel_launches(rrsph_solver* s, uint64_t* launches) {
     if (!s || !launches) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_kernel_launches: null argument");
     *launches = s->launches;
+    return RRSPH_OK;
+}
+
+// ------------------------------------------------- ensembles and tuning ----
+
+namespace {
+
+void drop_graphs(rrsph_solver* s) {
+    cudaStreamSynchronize(s->stream);
+    for (auto& g : s->graph) {
+        if (g) cudaGraphExecDestroy(g);
+        g = nullptr;
+    }
+}
+
+// A device copy of the particle state and step scalars (the autotuner runs
+// trial steps on the uploaded state and puts it back).
+struct Backup {
+    std::vector<std::pair<void*, size_t>> fields;
+    void* buf = nullptr;
+    rrsph::StepScalars scal[2];
+    uint64_t step_index = 0;
+};
+
+int backup_state(rrsph_solver* s, Backup& b) {
+    const size_t n = s->P.n, d = n * sizeof(double);
+    auto& S = s->S;
+    double* dbl[] = {S.rx, S.ry, S.rz, S.vx, S.vy, S.vz, S.ax, S.ay, S.az, S.avx, S.avy, S.avz,
+                     S.rho, S.p, S.drho, S.rho_pred};
+    for (double* f : dbl)
+        if (f) b.fields.emplace_back(f, d);
+    b.fields.emplace_back(S.itype, n * sizeof(int32_t));
+    size_t total = 0;
+    for (auto& f : b.fields) total += f.second;
+    RRSPH_CUDA_TRY(cudaMalloc(&b.buf, total));
+    char* dst = static_cast<char*>(b.buf);
+    for (auto& f : b.fields) {
+        RRSPH_CUDA_TRY(cudaMemcpyAsync(dst, f.first, f.second, cudaMemcpyDeviceToDevice, s->stream));
+        dst += f.second;
+    }
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(b.scal, s->scal, sizeof(b.scal), cudaMemcpyDeviceToHost, s->stream));
+    RRSPH_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    b.step_index = s->step_index;
+    return RRSPH_OK;
+}
+
+int restore_state(rrsph_solver* s, const Backup& b) {
+    const char* src = static_cast<const char*>(b.buf);
+    for (auto& f : b.fields) {
+        RRSPH_CUDA_TRY(cudaMemcpyAsync(f.first, src, f.second, cudaMemcpyDeviceToDevice, s->stream));
+        src += f.second;
+    }
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(s->scal, b.scal, sizeof(b.scal), cudaMemcpyHostToDevice, s->stream));
+    RRSPH_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->step_index = b.step_index;
+    s->keys_ready = false;
+    return RRSPH_OK;
+}
+
+}  // namespace
+
+extern "C" int rrsph_set_wave_makers(rrsph_solver* s, uint32_t count, const rrsph_wave_maker* makers) {
+    int rc = check_handle(s, "rrsph_set_wave_makers");
+    if (rc) return rc;
+    if (count && !makers) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_set_wave_makers: null makers");
+    const size_t n = s->P.n;
+    std::vector<int32_t> owner(n, -1);
+    std::vector<rrsph::PistonLaw> laws(count);
+    const double g = s->params.g, pi = s->params.pi;
+    for (uint32_t w = 0; w < count; w++) {
+        const rrsph_wave_maker& m = makers[w];
+        if ((m.nwm != 2 && m.nwm != 3) || m.particles_end < m.particles_start || m.particles_end > n ||
+            !(m.wave_length > 0) || !(m.depth > 0))
+            return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_set_wave_makers: bad wave maker " + std::to_string(w));
+        for (uint64_t i = m.particles_start; i < m.particles_end; i++) {
+            if (owner[i] >= 0)
+                return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_set_wave_makers: overlapping particle ranges");
+            owner[i] = (int32_t)w;
+        }
+        // nwm_wave_number and nwm_freq as fillInComputingParams derives them (Input.cpp:125-137)
+        const double k = 2. * pi / m.wave_length;
+        const double kd = k * m.depth;
+        laws[w] = rrsph::PistonLaw{(int)m.nwm, m.time_start, m.phase, std::sqrt(k * g * std::tanh(kd)),
+                                   m.wave_magnitude, k, m.depth};
+    }
+    drop_graphs(s);  // the step graphs hold the state pointers by value
+    if (!s->S.wave_tank) {
+        if ((rc = dev_alloc(s, &s->S.wave_tank, n)) != 0) return rc;
+    }
+    rrsph::PistonLaw* table = nullptr;
+    if ((rc = dev_alloc(s, &table, std::max<size_t>(count, 1))) != 0) return rc;
+    RRSPH_CUDA_TRY(cudaMemcpy(s->S.wave_tank, owner.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice));
+    if (count) RRSPH_CUDA_TRY(cudaMemcpy(table, laws.data(), count * sizeof(rrsph::PistonLaw), cudaMemcpyHostToDevice));
+    s->S.wave_law = table;
+    if (!count) s->S.wave_tank = nullptr;  // an empty table restores the params' wave maker
+    return RRSPH_OK;
+}
+
+extern "C" int rrsph_set_gather_threads(rrsph_solver* s, uint32_t density_threads, uint32_t force_threads) {
+    int rc = check_handle(s, "rrsph_set_gather_threads");
+    if (rc) return rc;
+    for (uint32_t t : {density_threads, force_threads})
+        if (t == 0 || t % 32 || t > (uint32_t)rrsph::kMaxGatherThreads)
+            return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_set_gather_threads: block size must be a multiple of "
+                                                         "32 in [32, 256]");
+    drop_graphs(s);
+    s->gather_threads[0] = (int)density_threads;
+    s->gather_threads[1] = (int)force_threads;
+    return RRSPH_OK;
+}
+
+extern "C" int rrsph_autotune(rrsph_solver* s, uint32_t steps, uint32_t* threads_out) {
+    int rc = check_handle(s, "rrsph_autotune");
+    if (rc) return rc;
+    if (steps == 0) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_autotune: steps must be positive");
+    uint32_t flags_before = 0;
+    RRSPH_CUDA_TRY(cudaMemcpy(&flags_before, s->flags, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    Backup b;
+    if ((rc = backup_state(s, b)) != 0) {
+        if (b.buf) cudaFree(b.buf);
+        return rc;
+    }
+    const int cand[] = {64, 128, 256};
+    float best = 0;
+    int best_d = s->gather_threads[0], best_f = s->gather_threads[1];
+    cudaEvent_t e0 = s->ev[0], e1 = s->ev[1];
+    const bool timing = s->timing;
+    s->timing = false;
+    for (int td : cand) {
+        for (int tf : cand) {
+            drop_graphs(s);
+            s->gather_threads[0] = td;
+            s->gather_threads[1] = tf;
+            rc = enqueue_steps(s, 1);  // captures the candidate's graphs
+            if (!rc) {
+                cudaEventRecord(e0, s->stream);
+                rc = enqueue_steps(s, steps);
+                cudaEventRecord(e1, s->stream);
+            }
+            if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = set_error(RRSPH_ERR_CUDA, "rrsph_autotune: event");
+            float ms = 0;
+            if (!rc) cudaEventElapsedTime(&ms, e0, e1);
+            if (!rc) rc = restore_state(s, b);
+            if (rc) break;
+            if (best == 0 || ms < best) {
+                best = ms;
+                best_d = td;
+                best_f = tf;
+            }
+        }
+        if (rc) break;
+    }
+    s->timing = timing;
+    cudaFree(b.buf);
+    drop_graphs(s);
+    s->gather_threads[0] = best_d;
+    s->gather_threads[1] = best_f;
+    if (rc) return rc;
+    if (threads_out) {
+        threads_out[0] = (uint32_t)best_d;
+        threads_out[1] = (uint32_t)best_f;
+    }
+    // flags the trial steps raised belong to no step the caller ran
+    RRSPH_CUDA_TRY(cudaMemcpy(s->flags, &flags_before, sizeof(uint32_t), cudaMemcpyHostToDevice));
     return RRSPH_OK;
 }

@@ -48,6 +48,7 @@ struct rrsph_solver {
     double phase_ms[kPhases] = {};
     uint64_t timed_steps = 0;
     rrsph_impl::AdjointRun* adj = nullptr;
+    int gather_threads[2] = {rrsph::kGatherThreads, rrsph::kGatherThreads};  // density, forces block sizes
 };
 
 namespace rrsph_impl {

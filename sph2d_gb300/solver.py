@@ -211,6 +211,25 @@ class Solver:
         check(lib().rrsph_forces(self._h, terms, _dp(a), self.dim, _dp(av), _dp(mu)))
         return a, av, mu
 
+    # -- ensembles and tuning
+    def set_wave_makers(self, makers) -> None:
+        """Pistons of a packed ensemble: dicts with particles_start, particles_end,
+        nwm, time_start, phase, wave_length, wave_magnitude, depth."""
+        arr = (capi.RrsphWaveMaker * max(len(makers), 1))()
+        for i, m in enumerate(makers):
+            for k, v in m.items():
+                setattr(arr[i], k, v)
+        check(lib().rrsph_set_wave_makers(self._h, len(makers), arr))
+
+    def set_gather_threads(self, density: int, forces: int) -> None:
+        check(lib().rrsph_set_gather_threads(self._h, density, forces))
+
+    def autotune(self, steps: int = 5):
+        """Picks the gather block sizes by timing; returns (density, forces) threads."""
+        out = (C.c_uint32 * 2)()
+        check(lib().rrsph_autotune(self._h, steps, out))
+        return int(out[0]), int(out[1])
+
     # -- piston optimisation
     def set_piston_fourier(self, omega: float, coef) -> None:
         """Piston displacement X(t) = sum_k coef[k-1] sin(k omega t) (empty coef: the wave maker's own law)."""
