@@ -36,6 +36,7 @@ struct DevParams {
     uint32_t max_nb;        // max_neighbours: the reference stores at most max_nb - 1
     int type_non_existent;
     double xmin, ymin, zmin, xmax, ymax, zmax;
+    long long oxmin, oymin, ozmin, oxmax, oymax, ozmax;  // dorder() of the bounds
     double cell;            // cell_scale_k * hsml (grid_cell_size)
     double inv_cell;
     double cut2;            // sqr(grid_cell_size()) computed as the reference does
@@ -96,6 +97,61 @@ struct StepScalars {
     unsigned long long pairs_total;  // pairs summed over the steps since upload
 };
 
+// ------------------------------------------- FP64-free double handling --
+// The FP64 pipe is the scarce one on this part (one lane per clock per SM), so
+// compares, halvings and conversions of doubles that need no FP64 arithmetic
+// are done on their bit patterns with integer operations.
+
+// Integer image of a double that orders like the double (IEEE total order with
+// -0 mapped to +0, so equal zeros stay equal). NaNs are excluded by callers.
+__host__ __device__ inline long long dorder(double v) {
+    long long b;
+#ifdef __CUDA_ARCH__
+    b = __double_as_longlong(v);
+#else
+    __builtin_memcpy(&b, &v, sizeof(b));
+#endif
+    if (b == (long long)0x8000000000000000ull) b = 0;
+    return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFll);
+}
+__device__ __forceinline__ bool dnan(double v) {
+    return ((unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull;
+}
+// v / 2, exactly, for a normal v whose half is normal; otherwise the multiply.
+__device__ __forceinline__ double dhalf(double v) {
+    const long long b = __double_as_longlong(v);
+    const long long e = (b >> 52) & 0x7FF;
+    if (e > 1 && e < 0x7FF) return __longlong_as_double(b - (1ll << 52));
+    return v * 0.5;
+}
+// Round-to-nearest-even double -> float (bit-identical to the conversion
+// instruction) for results in the normal float range; the rest converts in hardware.
+__device__ __forceinline__ float d2f(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned int e = (unsigned int)(b >> 52) & 0x7FFu;
+    if (e >= 1023u - 126u && e <= 1023u + 127u) {
+        const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+        const unsigned int mf = (unsigned int)((b >> 29) & 0x7FFFFFu);
+        const unsigned int rem = (unsigned int)(b & 0x1FFFFFFFu);
+        unsigned int r = ((e - 1023u + 127u) << 23) | mf;
+        if (rem > 0x10000000u || (rem == 0x10000000u && (mf & 1u))) r += 1;  // a carry moves to the next binade or to inf
+        return __uint_as_float(sign | r);
+    }
+    return (float)v;
+}
+// Exact float -> double for normal floats; the rest converts in hardware.
+__device__ __forceinline__ double f2d(float f) {
+    const unsigned int b = __float_as_uint(f);
+    const unsigned int e = (b >> 23) & 0xFFu;
+    if (e != 0u && e != 0xFFu) {
+        const unsigned long long r = ((unsigned long long)(b & 0x80000000u) << 32) |
+                                     ((unsigned long long)(e - 127u + 1023u) << 52) |
+                                     ((unsigned long long)(b & 0x7FFFFFu) << 29);
+        return __longlong_as_double((long long)r);
+    }
+    return (double)f;
+}
+
 // ---------------------------------------------------------------- Morton --
 // GridUtils.h:50-64 and 92-104, computed in 64-bit like rr_uint.
 __host__ __device__ inline uint64_t split2(uint64_t x) {
@@ -141,18 +197,39 @@ __device__ inline uint64_t cell_coord(double r, double rmin, double cell) {
     return (uint64_t)c;
 }
 
-// The same truncation with a multiply by 1/cell instead of the division. The
-// product is within 2 ulp of the correctly rounded quotient, so the two
-// truncate alike unless the quotient lies within 1e-9 of an integer; there the
-// exact division decides.
-__device__ inline uint64_t cell_coord_fast(double r, double rmin, double cell, double inv_cell) {
-    const double d = __dsub_rn(r, rmin);
-    const double q = __dmul_rn(d, inv_cell);
-    if (!(q >= 0.0) || !(q < 4.0e9)) return cell_coord(r, rmin, cell);
-    const double t = trunc(q);
-    const double frac = q - t;
-    if (frac > 1e-9 && frac < 1.0 - 1e-9) return (uint64_t)t;
-    return cell_coord(r, rmin, cell);
+// Cell coordinate of r (the truncation above) and r's offset from that
+// cell's lower edge, from one double subtract and one multiply. The FP64 pipe
+// is the scarce one, so the integer part and the fraction of
+// q = (r - rmin) * (1/cell) are read from q's bits with integer operations.
+// q is within 2 ulp of the exact quotient, so where 2^-30 <= q < 2^21 and q's
+// fraction is more than 2^-30 from an integer its truncation is the
+// quotient's; every other case (outside the geometry, near a cell edge, not
+// finite) takes the exact division. below: r < rmin or r is NaN.
+struct CellSplit {
+    uint64_t c;
+    float off;   // r - (rmin + c cell), in float
+    bool below;
+};
+__device__ inline CellSplit cell_split(double r, double rmin, double cell, double inv_cell, float cellf) {
+    const double q = __dmul_rn(__dsub_rn(r, rmin), inv_cell);
+    const long long bits = __double_as_longlong(q);
+    if (bits > 0) {
+        const int e = (int)(bits >> 52) - 1023;
+        const unsigned long long m = ((unsigned long long)bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+        if (e >= 0 && e <= 20) {
+            const int F = 52 - e;
+            const unsigned long long frac = m & ((1ull << F) - 1);
+            const unsigned long long top = frac >> (F - 30);
+            if (top != 0 && top != (1ull << 30) - 1) {
+                const float f = (float)(uint32_t)(frac >> (F - 24)) * 5.9604644775390625e-8f;  // * 2^-24
+                return {m >> F, f * cellf, false};
+            }
+        } else if (e < 0 && e >= -30 && !(e == -1 && (m >> 23) == (1ull << 30) - 1)) {
+            return {0, (float)q * cellf, false};
+        }
+    }
+    const uint64_t c = cell_coord(r, rmin, cell);
+    return {c, (float)(r - (rmin + (double)c * cell)), !(r >= rmin)};
 }
 
 // Neighbour-cell coordinate steps (GridUtils.h:158-163).

@@ -21,6 +21,11 @@ struct State {
     uint32_t* key_of;          // cell key used by the last grid build, per id
     int32_t* wave_tank;        // piston of each particle in wave_law, -1 for none (null: the params' wave maker)
     const PistonLaw* wave_law; // wave-maker table
+    // FP32-mixed step only (null otherwise), written by the key pass, id order:
+    float2* coff2;             // 2D: offset of r from its cell's lower edge
+    float4* coff4;             // 3D: the same (x, y, z)
+    float2* vpf2;              // 2D: v_predict in float
+    float4* vpf4;              // 3D: the same (x, y, z)
 };
 
 // Per-step cell-ordered copies and the grid.
@@ -55,6 +60,7 @@ struct GatherSrc {
     const double *vx, *vy, *vz;
     const double* rho;
     const double* p;  // pressure to copy (rrsph_forces on the given state); null in the loop
+    int loop;         // 1: the loop's mixed step (float v_predict from the key pass; no double copies)
 };
 
 template <int DIM>

@@ -16,19 +16,40 @@ inline unsigned blocks_for(uint32_t n, int threads) { return (n + threads - 1) /
 // max_cells-sized reset.
 // Cell key of particle i at (x, y, z) (GridFind.cpp:55-75); also clears the
 // previous grid's cell-table entry of i and records the new key.
+// Strictly inside the geometry box (WholeStep.cpp:4-17, ConsistencyCheck.cpp:162-218),
+// the double compares done on the ordered bit patterns (a NaN is outside).
 template <int DIM>
+__device__ __forceinline__ bool in_geometry(const DevParams& P, double x, double y, double z) {
+    const long long ox = dorder(x), oy = dorder(y);
+    bool in = ox < P.oxmax && ox > P.oxmin && oy < P.oymax && oy > P.oymin && !dnan(x) && !dnan(y);
+    if (DIM == 3) {
+        const long long oz = dorder(z);
+        in = in && oz < P.ozmax && oz > P.ozmin && !dnan(z);
+    }
+    return in;
+}
+
+// Compile-time variants of the per-particle kernels. A switch that is off in
+// a variant leaves no instructions behind: the FP64 pipe (one lane per clock
+// per SM on this part) also issues the predicated-off double instructions of
+// small if-converted branches.
+enum : int { kVarCont = 1, kVarRare = 2, kVarMixed = 4 };  // continuity, XSPH or dynamic dt, FP32-mixed
+// M: 0 = FP64 step, 1 = FP32-mixed step, 2 = decided at run time from the state's buffers.
+
+template <int DIM, int M>
 __device__ __forceinline__ void key_pass(const DevParams& P, const State& S, const Sorted& G, uint32_t i, double x,
                                          double y, double z, uint32_t* __restrict__ flags) {
-    bool outside = !(x >= P.xmin) || !(y >= P.ymin);
-    const uint64_t cx = cell_coord_fast(x, P.xmin, P.cell, P.inv_cell);
-    const uint64_t cy = cell_coord_fast(y, P.ymin, P.cell, P.inv_cell);
+    const CellSplit sx = cell_split(x, P.xmin, P.cell, P.inv_cell, P.mf.cell);
+    const CellSplit sy = cell_split(y, P.ymin, P.cell, P.inv_cell, P.mf.cell);
+    bool outside = sx.below || sy.below;
     uint64_t key;
+    CellSplit sz{0, 0.0f, false};
     if (DIM == 3) {
-        outside = outside || !(z >= P.zmin);
-        const uint64_t cz = cell_coord_fast(z, P.zmin, P.cell, P.inv_cell);
-        key = split3(cx) | (split3(cy) << 1) | (split3(cz) << 2);
+        sz = cell_split(z, P.zmin, P.cell, P.inv_cell, P.mf.cell);
+        outside = outside || sz.below;
+        key = split3(sx.c) | (split3(sy.c) << 1) | (split3(sz.c) << 2);
     } else {
-        key = split2(cx) | (split2(cy) << 1);
+        key = split2(sx.c) | (split2(sy.c) << 1);
     }
     if (key >= P.max_cells || outside) {
         // cell_idx >= max_cells (GridFind.cpp:61-72); keep kernels in bounds
@@ -40,16 +61,41 @@ __device__ __forceinline__ void key_pass(const DevParams& P, const State& S, con
     S.key_of[i] = (uint32_t)key;
     G.keys_in[i] = (uint32_t)key;
     G.ids_in[i] = i;
+    if (M == 0) return;
+    // offsets from the edge of the cell the key names: the Morton code keeps 16
+    // bits per axis in 2D and 10 in 3D (GridUtils.h:50-64, 92-104)
+    if (DIM == 2 && (M == 1 || S.coff2)) {
+        const float ox = sx.off + (float)(sx.c & ~0xFFFFull) * P.mf.cell;
+        const float oy = sy.off + (float)(sy.c & ~0xFFFFull) * P.mf.cell;
+        S.coff2[i] = make_float2(ox, oy);
+    } else if (DIM == 3 && (M == 1 || S.coff4)) {
+        const float ox = sx.off + (float)(sx.c & ~0x3FFull) * P.mf.cell;
+        const float oy = sy.off + (float)(sy.c & ~0x3FFull) * P.mf.cell;
+        const float oz = sz.off + (float)(sz.c & ~0x3FFull) * P.mf.cell;
+        S.coff4[i] = make_float4(ox, oy, oz, 0.0f);
+    }
 }
 
-// predict_half_step (PredictHalfStep.cpp:4-23) of particle i with time step dt.
-template <int DIM>
+// predict_half_step (PredictHalfStep.cpp:4-23) of particle i with time step
+// dt; the mixed step keeps v_predict in float only.
+template <int DIM, int M, bool CONT>
 __device__ __forceinline__ void predict(const DevParams& P, const State& S, uint32_t i, double vx, double vy,
                                         double vz, double rho, double dt) {
-    S.vpx[i] = vx + S.ax[i] * dt * 0.5;
-    S.vpy[i] = vy + S.ay[i] * dt * 0.5;
-    if (DIM == 3) S.vpz[i] = vz + S.az[i] * dt * 0.5;
-    if (P.density_treatment != 0) S.rho_pred[i] = rho + S.drho[i] * dt * 0.5;
+    const bool mixed = M == 1 || (M == 2 && (DIM == 2 ? S.vpf2 != nullptr : S.vpf4 != nullptr));
+    if (M != 0 && mixed) {  // v* = v + a dt/2 in float: the forces read it in float
+        const float hf = d2f(dhalf(dt));
+        if (DIM == 2) {
+            S.vpf2[i] = make_float2(fmaf(d2f(S.ax[i]), hf, d2f(vx)), fmaf(d2f(S.ay[i]), hf, d2f(vy)));
+        } else {
+            S.vpf4[i] = make_float4(fmaf(d2f(S.ax[i]), hf, d2f(vx)), fmaf(d2f(S.ay[i]), hf, d2f(vy)),
+                                    fmaf(d2f(S.az[i]), hf, d2f(vz)), 0.0f);
+        }
+    } else if (M != 1) {  // the reference's v + (a dt) * 0.5
+        S.vpx[i] = vx + __dmul_rn(S.ax[i], dt) * 0.5;
+        S.vpy[i] = vy + __dmul_rn(S.ay[i], dt) * 0.5;
+        if (DIM == 3) S.vpz[i] = vz + __dmul_rn(S.az[i], dt) * 0.5;
+    }
+    if (CONT) S.rho_pred[i] = rho + __dmul_rn(S.drho[i], dt) * 0.5;
 }
 
 template <int DIM>
@@ -57,56 +103,86 @@ __global__ void k_keys(DevParams P, State S, Sorted G, const StepScalars* __rest
                        uint32_t* __restrict__ flags) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    if (do_predict)
-        predict<DIM>(P, S, i, S.vx[i], S.vy[i], DIM == 3 ? S.vz[i] : 0.0, P.density_treatment ? S.rho[i] : 0.0,
-                     scal->dt);
-    key_pass<DIM>(P, S, G, i, S.rx[i], S.ry[i], DIM == 3 ? S.rz[i] : 0.0, flags);
+    if (do_predict) {
+        if (P.density_treatment)
+            predict<DIM, 2, true>(P, S, i, S.vx[i], S.vy[i], DIM == 3 ? S.vz[i] : 0.0, S.rho[i], scal->dt);
+        else
+            predict<DIM, 2, false>(P, S, i, S.vx[i], S.vy[i], DIM == 3 ? S.vz[i] : 0.0, 0.0, scal->dt);
+    }
+    key_pass<DIM, 2>(P, S, G, i, S.rx[i], S.ry[i], DIM == 3 ? S.rz[i] : 0.0, flags);
 }
 
 // Gathers the state into cell order and records each cell's [start, end) in
 // the sorted arrays (the cells_start table of make_grid, GridFind.cpp:77-87).
-template <int DIM>
-__global__ void k_reorder(DevParams P, State S, Sorted G, GatherSrc F, int mixed) {
+// R: 0 = FP64 gathers; 1 = the mixed loop with summation density; 2 = the
+// mixed loop with continuity density; 3 = mixed, outside the loop (the
+// velocities, density and pressure given by F, double copies for exports).
+template <int DIM, int R>
+__global__ void k_reorder(DevParams P, State S, Sorted G, GatherSrc F) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= P.n) return;
     const uint32_t key = G.key[k];
     const uint32_t id = G.id[k];
     if (k == 0 || G.key[k - 1] != key) G.cell_start[key] = k;
     if (k == P.n - 1 || G.key[k + 1] != key) G.cell_end[key] = k + 1;
-    const double x = S.rx[id], y = S.ry[id], z = DIM == 3 ? S.rz[id] : 0.0;
     const int32_t t = S.itype[id];
-    G.rx[k] = x;
-    G.ry[k] = y;
-    if (DIM == 3) G.rz[k] = z;
-    G.itype[k] = t;
-    const double fvx = F.vx[id], fvy = F.vy[id], fvz = DIM == 3 ? F.vz[id] : 0.0;
-    const double frho = F.rho[id];
-    const bool cont = P.density_treatment != 0;
-    if (!mixed) {
-        G.vx[k] = fvx;
-        G.vy[k] = fvy;
-        if (DIM == 3) G.vz[k] = fvz;
-        G.rho[k] = frho;
+    if (R == 0 || R == 3) {  // double copies: the FP64 gathers and the grid/neighbour exports
+        G.rx[k] = S.rx[id];
+        G.ry[k] = S.ry[id];
+        if (DIM == 3) G.rz[k] = S.rz[id];
+        G.itype[k] = t;
+    }
+    if (R == 0) {
+        G.vx[k] = F.vx[id];
+        G.vy[k] = F.vy[id];
+        if (DIM == 3) G.vz[k] = F.vz[id];
+        G.rho[k] = F.rho[id];
         if (F.p) G.p[k] = F.p[id];
-        if (cont) {
+        if (P.density_treatment != 0) {
             G.vdx[k] = S.vx[id];
             G.vdy[k] = S.vy[id];
             if (DIM == 3) G.vdz[k] = S.vz[id];
             G.rhod[k] = S.rho[id];
         }
-    } else {
-        uint64_t cx, cy, cz;
-        decode_key<DIM>(key, cx, cy, cz);
-        const float ox = (float)(x - (P.xmin + (double)cx * P.cell));
-        const float oy = (float)(y - (P.ymin + (double)cy * P.cell));
-        const float oz = DIM == 3 ? (float)(z - (P.zmin + (double)cz * P.cell)) : 0.0f;
-        G.P4[k] = make_float4(ox, oy, oz, __int_as_float(t));
-        G.V4[k] = make_float4((float)fvx, (float)fvy, (float)fvz, (float)frho);
-        if (F.p) G.PR[k] = make_float2((float)F.p[id], (float)(F.p[id] / (frho * frho)));
-        if (cont)  // the density deviation keeps rho_i - rho_j accurate in float
-            G.VD4[k] = make_float4((float)S.vx[id], (float)S.vy[id], DIM == 3 ? (float)S.vz[id] : 0.0f,
-                                   (float)(S.rho[id] - P.rho0));
+        return;
     }
+    // FP32-mixed: cell-relative offsets the key pass computed from the same positions
+    float ox, oy, oz = 0.0f;
+    if (DIM == 2) {
+        const float2 o = S.coff2[id];
+        ox = o.x;
+        oy = o.y;
+    } else {
+        const float4 o = S.coff4[id];
+        ox = o.x;
+        oy = o.y;
+        oz = o.z;
+    }
+    G.P4[k] = make_float4(ox, oy, oz, __int_as_float(t));
+    float fvx, fvy, fvz = 0.0f, frho = 0.0f;  // the loop's summation density writes .w itself
+    if (R != 3) {  // v_predict in float from the predictor
+        if (DIM == 2) {
+            const float2 v = S.vpf2[id];
+            fvx = v.x;
+            fvy = v.y;
+        } else {
+            const float4 v = S.vpf4[id];
+            fvx = v.x;
+            fvy = v.y;
+            fvz = v.z;
+        }
+        if (R == 2) frho = d2f(F.rho[id]);
+    } else {
+        fvx = d2f(F.vx[id]);
+        fvy = d2f(F.vy[id]);
+        if (DIM == 3) fvz = d2f(F.vz[id]);
+        frho = d2f(F.rho[id]);
+        if (F.p) G.PR[k] = make_float2(d2f(F.p[id]), d2f(F.p[id] / (F.rho[id] * F.rho[id])));
+    }
+    G.V4[k] = make_float4(fvx, fvy, fvz, frho);
+    if (R == 2 || (R == 3 && P.density_treatment != 0))  // rho - rho0 keeps rho_i - rho_j accurate in float
+        G.VD4[k] = make_float4(d2f(S.vx[id]), d2f(S.vy[id]), DIM == 3 ? d2f(S.vz[id]) : 0.0f,
+                               d2f(S.rho[id] - P.rho0));
 }
 
 // Piston velocity of dynamic_boundaries (RRSPH_OMP/src/WaveMaker.cpp:34-82)
@@ -161,13 +237,15 @@ __device__ double solitary_vx(const DevParams& P, double time) {
 // (RRSPH_OMP/src/WholeStep.cpp:19-62) + the per-step boundary check of
 // RRSPHOutput::update_step (RRSPH_COMMON/src/Output.cpp:395-416). Thread 0
 // advances the step scalars into scal_next (time += dt, step + 1).
-template <int DIM>
+template <int DIM, int V>
 __global__ void k_whole(DevParams P, State S, Sorted G, const StepScalars* __restrict__ scal,
                         StepScalars* __restrict__ next, uint32_t* __restrict__ flags, int next_keys) {
+    constexpr bool CONT = (V & kVarCont) != 0, RARE = (V & kVarRare) != 0;
+    constexpr int M = (V & kVarMixed) ? 1 : 0;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     // update_dt (UpdateAcceleration.cpp:15-29) under DT_CORRECTION_DYNAMIC
     double dt = scal->dt;
-    if (P.dt_method == 2) {
+    if (RARE && P.dt_method == 2) {
         const double amax = P.dt_reduce ? __longlong_as_double((long long)scal->amax_bits) : 0.0;
         const double mumax = P.dt_reduce ? __longlong_as_double((long long)scal->mumax_bits) : 0.0;
         const double min_dt_a = sqrt(P.h / amax);
@@ -188,7 +266,7 @@ __global__ void k_whole(DevParams P, State S, Sorted G, const StepScalars* __res
         next->pairs_total = scal->pairs_total + scal->pairs;
     }
     if (i >= P.n) return;
-    const bool waves = P.nwm && !nwm_off && time >= P.nwm_time_start;
+    const bool waves = P.nwm && !nwm_off && dorder(time) >= dorder(P.nwm_time_start);
     if (S.wave_tank) {  // a table of pistons (one per tank of an ensemble)
         const int32_t w = S.wave_tank[i];
         if (w >= 0) {
@@ -208,19 +286,20 @@ __global__ void k_whole(DevParams P, State S, Sorted G, const StepScalars* __res
             S.itype[i] = P.type_non_existent;
         }
     }
-    const double v_dt = scal->step ? dt : dt * 0.5;
+    const double v_dt = scal->step ? dt : dhalf(dt);
     double rho = 0.0;
-    if (P.density_treatment != 0) {
+    if (CONT) {
         rho = S.rho[i] + S.drho[i] * v_dt;
         S.rho[i] = rho;
     }
     double x = S.rx[i], y = S.ry[i], z = DIM == 3 ? S.rz[i] : 0.0;
     double vx = S.vx[i], vy = S.vy[i], vz = DIM == 3 ? S.vz[i] : 0.0;
+    bool in = true, in_known = false;  // the geometry test of the final position, once
     if (S.itype[i] > 0) {
         vx = vx + S.ax[i] * v_dt;
         vy = vy + S.ay[i] * v_dt;
         if (DIM == 3) vz = vz + S.az[i] * v_dt;
-        if (P.avg_vel) {
+        if (RARE && P.avg_vel) {
             vx += S.avx[i];
             vy += S.avy[i];
             if (DIM == 3) vz += S.avz[i];
@@ -230,11 +309,12 @@ __global__ void k_whole(DevParams P, State S, Sorted G, const StepScalars* __res
         if (DIM == 3) S.vz[i] = vz;
         const double nx = x + vx * dt, ny = y + vy * dt, nz = DIM == 3 ? z + vz * dt : 0.0;
         bool move = true;
-        if (P.consistency_treatment == 2) {  // CONSISTENCY_FIX (WholeStep.cpp:47-54)
-            bool in = nx < P.xmax && nx > P.xmin && ny < P.ymax && ny > P.ymin;
-            if (DIM == 3) in = in && nz < P.zmax && nz > P.zmin;
-            if (!in) {
+        if (P.consistency_treatment == 2 || P.consistency_check) {
+            in = in_geometry<DIM>(P, nx, ny, nz);
+            in_known = true;
+            if (P.consistency_treatment == 2 && !in) {  // CONSISTENCY_FIX (WholeStep.cpp:47-54)
                 move = false;
+                in_known = false;
                 S.itype[i] = P.type_non_existent;
             }
         }
@@ -246,14 +326,13 @@ __global__ void k_whole(DevParams P, State S, Sorted G, const StepScalars* __res
         }
     }
     if (P.consistency_check) {  // check_particles_are_within_boundaries (ConsistencyCheck.cpp:147-218)
-        bool in = x < P.xmax && x > P.xmin && y < P.ymax && y > P.ymin;
-        if (DIM == 3) in = in && z < P.zmax && z > P.zmin;
+        if (!in_known) in = in_geometry<DIM>(P, x, y, z);
         if (!in) atomicOr(flags, RRSPH_FLAG_OUTSIDE_GEOMETRY);
     }
     if (next_keys) {
         // the next step's predict_half_step and cell keys, from the state just written
-        predict<DIM>(P, S, i, vx, vy, vz, rho, dt);
-        key_pass<DIM>(P, S, G, i, x, y, z, flags);
+        predict<DIM, M, CONT>(P, S, i, vx, vy, vz, rho, dt);
+        key_pass<DIM, M>(P, S, G, i, x, y, z, flags);
     }
 }
 
@@ -344,12 +423,25 @@ void launch_keys(const DevParams& P, const State& S, Sorted& G, StepScalars* sca
 }
 template <int DIM>
 void launch_reorder(const DevParams& P, const State& S, const Sorted& G, GatherSrc fsrc, int mixed, cudaStream_t st) {
-    k_reorder<DIM><<<blocks_for(P.n, 256), 256, 0, st>>>(P, S, G, fsrc, mixed);
+    const unsigned b = blocks_for(P.n, 256);
+    if (!mixed) k_reorder<DIM, 0><<<b, 256, 0, st>>>(P, S, G, fsrc);
+    else if (!fsrc.loop) k_reorder<DIM, 3><<<b, 256, 0, st>>>(P, S, G, fsrc);
+    else if (P.density_treatment == 0) k_reorder<DIM, 1><<<b, 256, 0, st>>>(P, S, G, fsrc);
+    else k_reorder<DIM, 2><<<b, 256, 0, st>>>(P, S, G, fsrc);
 }
 template <int DIM>
 void launch_whole_step(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal_cur,
                        StepScalars* scal_next, uint32_t* flags, int next_keys, cudaStream_t st) {
-    k_whole<DIM><<<blocks_for(P.n, 256), 256, 0, st>>>(P, S, G, scal_cur, scal_next, flags, next_keys);
+    const int v = (P.density_treatment != 0 ? kVarCont : 0) | (P.avg_vel || P.dt_method == 2 ? kVarRare : 0) |
+                  ((DIM == 2 ? S.vpf2 != nullptr : S.vpf4 != nullptr) ? kVarMixed : 0);
+    const unsigned b = blocks_for(P.n, 256);
+    switch (v) {
+#define RRSPH_WHOLE(V) \
+    case V: k_whole<DIM, V><<<b, 256, 0, st>>>(P, S, G, scal_cur, scal_next, flags, next_keys); break;
+        RRSPH_WHOLE(0) RRSPH_WHOLE(1) RRSPH_WHOLE(2) RRSPH_WHOLE(3)
+        RRSPH_WHOLE(4) RRSPH_WHOLE(5) RRSPH_WHOLE(6) RRSPH_WHOLE(7)
+#undef RRSPH_WHOLE
+    }
 }
 void launch_cells_start(const DevParams& P, const Sorted& G, uint32_t* out, cudaStream_t st) {
     const uint64_t m = (uint64_t)P.max_cells + 1;

@@ -27,7 +27,7 @@ struct Kahan {
         c = (t - s) - y;
         s = t;
     }
-    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+    __device__ __forceinline__ double value() const { return f2d(s) - f2d(c); }
 };
 
 // W(q) of smoothing kernel skf (SmoothingKernel.h:20-252), float.
@@ -75,12 +75,15 @@ __device__ __forceinline__ float kernel_dwdr_scalef(int skf, float f, float q, f
 }
 
 // Cutoff test: float test outside the guard band, the reference's double test inside it.
+// The guard band is rare, so its double positions come from the id-order state.
 template <int DIM>
-__device__ __forceinline__ bool within_cutoff(const DevParams& P, const Sorted& G, uint32_t i, uint32_t k, float d2) {
+__device__ __forceinline__ bool within_cutoff(const DevParams& P, const State& S, const Sorted& G, uint32_t i,
+                                              uint32_t k, float d2) {
     if (d2 >= P.mf.cut2_hi) return false;
     if (d2 < P.mf.cut2_lo) return true;
-    const double dx = __dsub_rn(G.rx[i], G.rx[k]), dy = __dsub_rn(G.ry[i], G.ry[k]);
-    const double dz = DIM == 3 ? __dsub_rn(G.rz[i], G.rz[k]) : 0.0;
+    const uint32_t a = G.id[i], b = G.id[k];
+    const double dx = __dsub_rn(S.rx[a], S.rx[b]), dy = __dsub_rn(S.ry[a], S.ry[b]);
+    const double dz = DIM == 3 ? __dsub_rn(S.rz[a], S.rz[b]) : 0.0;
     return exact_dist2<DIM>(dx, dy, dz) < P.cut2;
 }
 
@@ -154,7 +157,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_mixed(DevParams P
                     if (__float_as_int(pi.w) == P.type_non_existent) continue;
                     const float dx = pi.x + shx, dy = pi.y + shy, dz = DIM == 3 ? pi.z + shz : 0.0f;
                     const float d2 = DIM == 3 ? dx * dx + dy * dy + dz * dz : dx * dx + dy * dy;
-                    if (!within_cutoff<DIM>(P, G, i, k, d2)) continue;
+                    if (!within_cutoff<DIM>(P, S, G, i, k, d2)) continue;
                     cnt++;
                     if (i - s < 32) bits |= 1u << (i - s);
                     const float inv_dist = rsqrtf(d2);
@@ -214,8 +217,8 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_mixed(DevParams P
             const float pr = eos_pf(M, d);
             G.V4[k].w = rho;
             G.PR[k] = make_float2(pr, pr * __frcp_rn(rho * rho));
-            S.rho[id] = P.rho0 + (double)d;
-            S.p[id] = pr;
+            S.rho[id] = P.rho0 + f2d(d);
+            S.p[id] = f2d(pr);
         } else {
             const float d = (float)(S.rho[id] - P.rho0);
             const float pr = eos_pf(M, d);
@@ -381,7 +384,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_forces_mixed(DevParams P,
                     if (ti == P.type_non_existent) continue;
                     const float dx = pi4.x + hx, dy = pi4.y + hy;
                     const float d2 = dx * dx + dy * dy;
-                    if (!within_cutoff<DIM>(P, G, i, k, d2)) continue;
+                    if (!within_cutoff<DIM>(P, S, G, i, k, d2)) continue;
                     F.pair(i, dx, dy, 0.0f, d2, ti);
                 }
                 ax.add(F.cax);
@@ -413,7 +416,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_forces_mixed(DevParams P,
                     if (ti == P.type_non_existent) continue;
                     const float dx = pi4.x + shx, dy = pi4.y + shy, dz = DIM == 3 ? pi4.z + shz : 0.0f;
                     const float d2 = DIM == 3 ? dx * dx + dy * dy + dz * dz : dx * dx + dy * dy;
-                    if (!within_cutoff<DIM>(P, G, i, k, d2)) continue;
+                    if (!within_cutoff<DIM>(P, S, G, i, k, d2)) continue;
                     F.pair(i, dx, dy, dz, d2, ti);
                 }
                 ax.add(F.cax);

@@ -82,6 +82,8 @@ int fill_dev_params(const rrsph_params& p, rrsph::DevParams& P) {
     P.max_nb = p.max_neighbours;
     P.type_non_existent = p.type_non_existent;
     P.xmin = p.x_mingeom; P.ymin = p.y_mingeom; P.zmin = p.z_mingeom;
+    P.oxmin = rrsph::dorder(p.x_mingeom); P.oymin = rrsph::dorder(p.y_mingeom); P.ozmin = rrsph::dorder(p.z_mingeom);
+    P.oxmax = rrsph::dorder(p.x_maxgeom); P.oymax = rrsph::dorder(p.y_maxgeom); P.ozmax = rrsph::dorder(p.z_maxgeom);
     P.xmax = p.x_maxgeom; P.ymax = p.y_maxgeom; P.zmax = p.z_maxgeom;
     P.cell = p.cell_scale_k * p.hsml;
     P.inv_cell = 1.0 / P.cell;
@@ -218,7 +220,7 @@ void enqueue_step(rrsph_solver* s, int par, cudaEvent_t* events, bool with_keys)
     rrsph::StepScalars* cur = s->scal + par;
     rrsph::StepScalars* nxt = s->scal + (par ^ 1);
     const bool cont = s->P.density_treatment != 0;
-    rrsph::GatherSrc fsrc{s->S.vpx, s->S.vpy, s->S.vpz, cont ? s->S.rho_pred : s->S.rho, nullptr};
+    rrsph::GatherSrc fsrc{s->S.vpx, s->S.vpy, s->S.vpz, cont ? s->S.rho_pred : s->S.rho, nullptr, 1};
     if (events) cudaEventRecord(events[0], s->stream);
     if (with_keys) {
         rrsph::launch_keys<DIM>(s->P, s->S, s->G, cur, 1, s->flags, s->stream);
@@ -335,6 +337,7 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
         A(G.rho, n); A(G.p, n);
         if (cont) { A(G.vdx, n); A(G.vdy, n); if (d3) A(G.vdz, n); A(G.rhod, n); }
     } else {
+        if (d3) { A(S.coff4, n); A(S.vpf4, n); } else { A(S.coff2, n); A(S.vpf2, n); }
         A(G.P4, n); A(G.V4, n); A(G.PR, n);
         if (!d3) A(G.nbmask, 10 * n);
         if (cont) A(G.VD4, n);
@@ -574,7 +577,7 @@ namespace {
 template <int DIM>
 void enqueue_component_grid(rrsph_solver* s, bool with_p) {
     s->keys_ready = false;  // this grid's keys were made without the predictor
-    rrsph::GatherSrc fsrc{s->S.vx, s->S.vy, s->S.vz, s->S.rho, with_p ? s->S.p : nullptr};
+    rrsph::GatherSrc fsrc{s->S.vx, s->S.vy, s->S.vz, s->S.rho, with_p ? s->S.p : nullptr, 0};
     enqueue_grid<DIM>(s, 0, s->scal, fsrc);
 }
 void enqueue_component_grid_dim(rrsph_solver* s, bool with_p) {

@@ -452,3 +452,40 @@ def test_stepping_in_chunks_equals_one_call(gpu_available):
     assert t == t2
     for k in ("r", "v", "rho", "p"):
         assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cell_keys_at_cell_edges(gpu_available, precision):
+    """Positions on, a few ulp either side of, and 2^-30 cell from cell edges,
+    and on the geometry minimum: the key pass reads q = (r - rmin)/cell from
+    its bits and must truncate exactly like the reference's division
+    (GridUtils.h:135-150)."""
+    from oracle import binding as O
+    from sph2d_gb300 import Solver
+
+    case = _dam(nx=20, ny=10)
+    p = case.params()
+    cell = p.cell_scale_k * p.hsml
+    rng = np.random.default_rng(5)
+    n = case.ntotal
+    cmax = (int((p.x_maxgeom - p.x_mingeom) / cell) - 1, int((p.y_maxgeom - p.y_mingeom) / cell) - 1)
+    r = np.empty((n, 2))
+    for d, lo in enumerate((p.x_mingeom, p.y_mingeom)):
+        c = rng.integers(1, cmax[d], n)  # (below the geometry minimum is an error, tested elsewhere)
+        k = rng.integers(-4, 5, n)
+        edge = lo + c * cell
+        x = edge.copy()
+        for j in range(n):
+            if abs(k[j]) == 4:
+                x[j] = edge[j] + np.sign(k[j]) * cell * 2.0 ** -30
+            else:
+                for _ in range(abs(k[j])):
+                    x[j] = np.nextafter(x[j], np.sign(k[j]) * np.inf)
+        r[:, d] = x
+    r[0] = [p.x_mingeom, p.y_mingeom]
+    with Solver(p, precision) as s:
+        s.upload(r, case.v, case.rho, case.itype)
+        keys, grid, _ = s.grid_find()
+    ref_keys, ref_grid, _ = O.grid(p, r)
+    assert np.array_equal(keys, ref_keys)
+    assert np.array_equal(grid, ref_grid)
