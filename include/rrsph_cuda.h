@@ -283,7 +283,7 @@ int rrsph_forces(rrsph_solver* s, uint32_t terms, double* a, uint32_t stride,
  * can block or fail mid-run). No counterpart in the reference.
  * Every pointer is a device pointer owned by the caller; outputs must not
  * overlap inputs, and the inputs are left unchanged. The working memory is a
- * fixed array inside the library (about 8.9 MB; every GPU that loads the
+ * fixed array inside the library (about 9.4 MB; every GPU that loads the
  * library holds it until the process exits), so n is limited to
  * RRSPH_SORT_NOALLOC_MAX_PAIRS and a larger n returns
  * RRSPH_ERR_INVALID_ARGUMENT. The call allocates nothing and is asynchronous

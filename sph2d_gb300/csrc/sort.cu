@@ -7,7 +7,7 @@
 // reference's reverse scatter.
 //
 // One 8-bit digit per pass, three kernels per pass, no inter-block waiting:
-//   1. k_tile_hist:   digit counts of each 2048-key tile        -> counts[d][tile]
+//   1. k_tile_hist:   digit counts of each 1024-key tile        -> counts[d][tile]
 //   2. k_digit_scan:  one warp per digit scans its row over tiles (exclusive)
 //                     and records the digit total
 //   3. k_scatter:     each tile ranks its keys stably (warp match + per-warp

@@ -7,7 +7,7 @@
 namespace rrsph {
 
 constexpr int kSortThreads = 256;
-constexpr int kSortItems = 8;
+constexpr int kSortItems = 4;
 constexpr int kSortTile = kSortThreads * kSortItems;  // keys per tile
 constexpr int kRadix = 256;                           // 8-bit digits
 

@@ -10,7 +10,7 @@
 //
 // The array holds one spare key/id buffer pair for the ping-pong passes plus
 // the per-tile digit counts, sized for RRSPH_SORT_NOALLOC_MAX_PAIRS pairs
-// (about 8.9 MB). Every GPU that loads this library holds it until the process
+// (about 9.4 MB). Every GPU that loads this library holds it until the process
 // exits. Nothing in it needs clearing between calls: every pass rewrites the
 // counts it reads. All calls on a device share it, so calls that can overlap on
 // the GPU race; the caller orders them (one stream, or events).
