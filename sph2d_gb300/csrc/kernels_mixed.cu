@@ -270,17 +270,17 @@ struct ForceAcc {
             m += sc * pf * M.mass;
         }
         if (visc) {
+            // approaching pairs only (vr < 0); evaluated by every lane and masked,
+            // so the lanes of a warp stay together
             float vr = -((vj.x - vi.x) * dx + (vj.y - vi.y) * dy);
             if (DIM == 3) vr -= (vj.z - vi.z) * dz;
-            if (vr < 0) {
-                const float mu = __fdividef(M.h * vr, d2 + M.etq_h2);
-                arvmu = fmaxf(arvmu, fabsf(mu));
-                const float piv = __fdividef((M.av_beta * mu - M.av_alpha_c) * mu, 0.5f * (rhoi + rhoj));
-                const float sca = (SKF || av_skf == intf_skf)
-                                      ? sc
-                                      : kernel_dwdr_scalef(av_skf, M.kf[av_skf], q, inv_dist, M.inv_h);
-                m += sca * piv * M.mass;
-            }
+            const float mu = fminf(__fdividef(M.h * vr, d2 + M.etq_h2), 0.0f);
+            arvmu = fmaxf(arvmu, -mu);
+            const float piv = __fdividef((M.av_beta * mu - M.av_alpha_c) * mu, 0.5f * (rhoi + rhoj));
+            const float sca = (SKF || av_skf == intf_skf)
+                                  ? sc
+                                  : kernel_dwdr_scalef(av_skf, M.kf[av_skf], q, inv_dist, M.inv_h);
+            m += sca * piv * M.mass;
         }
         cax += dx * m;
         cay += dy * m;
