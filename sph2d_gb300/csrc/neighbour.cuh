@@ -128,6 +128,23 @@ struct Stencil {
     static __device__ __forceinline__ uint32_t pick(int i, const uint32_t* v) { return i == 0 ? v[0] : (i == 1 ? v[1] : v[2]); }
     static __device__ __forceinline__ int pick(int i, const int* v) { return i == 0 ? v[0] : (i == 1 ? v[1] : v[2]); }
 
+    // Coordinate offsets of stencil cell c (as cell() returns them).
+    __device__ __forceinline__ void offsets(int c, int& dx, int& dy, int& dz) const {
+        int a, b, d;
+        if (DIM == 3) {
+            a = c / 9;
+            b = (c / 3) % 3;
+            d = c % 3;
+        } else {
+            a = c / 3;
+            b = c % 3;
+            d = 1;
+        }
+        dx = pick(a, sx);
+        dy = pick(b, sy);
+        dz = DIM == 3 ? pick(d, sz) : 0;
+    }
+
     // Cell c of the stencil (c in [0, 3^DIM)); false when the reference marks
     // it invalid or its key is >= max_cells.
     __device__ __forceinline__ bool cell(int c, uint32_t& key, int& dx, int& dy, int& dz) const {
