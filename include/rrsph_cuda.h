@@ -360,6 +360,17 @@ int rrsph_set_gather_threads(rrsph_solver* s, uint32_t density_threads, uint32_t
  * state back. threads_out[2] (may be NULL) receives {density, forces}. */
 int rrsph_autotune(rrsph_solver* s, uint32_t steps, uint32_t* threads_out);
 
+/* Neighbour reuse of the 2D FP32-mixed step with summation density (on by
+ * default there): each particle's candidate list holds the particles within
+ * (cell_scale_k + skin_over_h) * hsml of it at the last grid build, and the
+ * grid and lists are rebuilt only when a particle has moved more than half the
+ * skin since then, so every pair within the cutoff stays in the lists. Each
+ * step still applies the reference's cutoff test to the list: the pairs are
+ * the reference's. RRSPH_ERR_UNSUPPORTED for other solvers. */
+int rrsph_set_neighbour_reuse(rrsph_solver* s, int enable, double skin_over_h);
+/* Grid + list rebuilds since the solver was created (0 without reuse). */
+int rrsph_neighbour_rebuilds(rrsph_solver* s, uint64_t* rebuilds);
+
 /* ---- timing hooks for benchmarks ------------------------------------------ */
 /* Number of kernel phases one step launches and their names. */
 int rrsph_phase_count(rrsph_solver* s, int* count);

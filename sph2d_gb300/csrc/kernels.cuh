@@ -26,6 +26,11 @@ struct State {
     float4* coff4;             // 3D: the same (x, y, z)
     float2* vpf2;              // 2D: v_predict in float
     float4* vpf4;              // 3D: the same (x, y, z)
+    // 2D mixed step with neighbour reuse (null otherwise), id order:
+    uint32_t* cxy;             // cell coordinates of the current position, x | y << 16
+    uint32_t* bcxy;            // cell coordinates at the last list build
+    float2* boff;              // offset from that cell's edge at the last list build
+    uint32_t* vl_rebuild;      // non-zero: the next step rebuilds the grid and the lists
 };
 
 // Per-step cell-ordered copies and the grid.
@@ -53,6 +58,15 @@ struct Sorted {
     // stencil cell c is a neighbour; word 9 = stencil cells with more than 32
     // particles (searched again by the force pass). Null where unused.
     uint32_t* nbmask;
+    // 2D mixed step with neighbour reuse: per particle a row of kVerletCap
+    // candidates (list[k * kVerletCap + e] = sorted index | cell code << 27,
+    // code = (dx + 2) * 5 + (dy + 2) for the candidate's cell offset; the last
+    // group of four is padded with kVlNone), vcount[k] = candidates (kListOver:
+    // too many, searched instead), vmask[k] = the candidates within the cutoff
+    // in this step.
+    uint32_t* vlist;
+    uint32_t* vcount;
+    unsigned long long* vmask;
 };
 
 // Sources the reorder gathers for the force velocity / density.
@@ -87,6 +101,18 @@ template <int DIM>
 void launch_whole_step(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal_cur,
                        StepScalars* scal_next, uint32_t* flags, int next_keys, cudaStream_t st);
 
+// Neighbour reuse (2D mixed step with summation density): the candidate lists
+// are built with the cutoff widened by a skin and reused while no particle has
+// moved more than half the skin since the build (kernels_mixed.cu).
+void launch_verlet_decide(cudaGraphConditionalHandle h, const uint32_t* rebuild, cudaStream_t st);
+void launch_verlet_reset(uint32_t* rebuild, unsigned long long* builds, cudaStream_t st);
+void launch_verlet_build(const DevParams& P, const State& S, const Sorted& G, cudaStream_t st);
+void launch_verlet_reorder(const DevParams& P, const State& S, const Sorted& G, cudaStream_t st);
+void launch_density_verlet(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
+                           cudaStream_t st, int threads);
+void launch_forces_verlet(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
+                          cudaStream_t st, int threads);
+
 void launch_cells_start(const DevParams& P, const Sorted& G, uint32_t* out, cudaStream_t st);
 template <int DIM>
 void launch_neighbour_list(const DevParams& P, const Sorted& G, uint32_t* counts, uint32_t* list, uint32_t max_per,
@@ -96,6 +122,9 @@ void launch_unpack(const DevParams& P, State S, const double* r, const double* v
 template <int DIM>
 void launch_pack(const DevParams& P, State S, double* r, double* v, uint32_t stride, cudaStream_t st);
 
+constexpr int kVerletCap = 64;          // candidate-list entries per particle (one 64-bit mask)
+constexpr uint32_t kListOver = 0xFFFFFFFFu;
+constexpr uint32_t kVlNone = 0xFFFFFFFFu;  // padding of a list row (never an entry)
 constexpr int kGatherThreads = 128;     // default block size of the pair gathers
 constexpr int kMaxGatherThreads = 256;
 

@@ -68,6 +68,18 @@ __device__ __forceinline__ void key_pass(const DevParams& P, const State& S, con
         const float ox = sx.off + (float)(sx.c & ~0xFFFFull) * P.mf.cell;
         const float oy = sy.off + (float)(sy.c & ~0xFFFFull) * P.mf.cell;
         S.coff2[i] = make_float2(ox, oy);
+        if (S.cxy) {  // neighbour reuse: the current cell, and the displacement since the list build
+            const uint32_t cx = (uint32_t)(sx.c & 0xFFFFu), cy = (uint32_t)(sy.c & 0xFFFFu);
+            S.cxy[i] = cx | (cy << 16);
+            const uint32_t b = S.bcxy[i];
+            const float2 bo = S.boff[i];
+            const float dx = ox + (float)((int)cx - (int)(b & 0xFFFFu)) * P.mf.cell - bo.x;
+            const float dy = oy + (float)((int)cy - (int)(b >> 16)) * P.mf.cell - bo.y;
+            const bool moved = !(dx * dx + dy * dy <= P.vl_half_skin2);
+            const unsigned am = __activemask();
+            const unsigned who = __ballot_sync(am, moved);
+            if (who && (threadIdx.x & 31) == (unsigned)(__ffs(am) - 1)) atomicOr(S.vl_rebuild, 1u);
+        }
     } else if (DIM == 3 && (M == 1 || S.coff4)) {
         const float ox = sx.off + (float)(sx.c & ~0x3FFull) * P.mf.cell;
         const float oy = sy.off + (float)(sy.c & ~0x3FFull) * P.mf.cell;

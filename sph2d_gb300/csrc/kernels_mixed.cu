@@ -19,6 +19,9 @@ namespace rrsph {
 
 namespace {
 
+constexpr int kVlBatch = 4;       // list entries the reuse density gather loads together (one uint4)
+constexpr int kVlForceBatch = 2;  // neighbours the reuse force gather loads together
+
 struct Kahan {
     float s, c;
     __device__ __forceinline__ void add(float x) {
@@ -245,6 +248,11 @@ struct ForceAcc {
     float cax, cay, caz, cvx, cvy, cvz, arvmu;
 
     __device__ __forceinline__ void pair(uint32_t i, float dx, float dy, float dz, float d2, int32_t ti) {
+        pair_with(G.V4[i], G.PR[i], dx, dy, dz, d2, ti);
+    }
+    // The same with neighbour i's velocity + density (vi) and pressure pair (pri) given.
+    __device__ __forceinline__ void pair_with(const float4 vi, const float2 pri, float dx, float dy, float dz,
+                                              float d2, int32_t ti) {
         const MixedF& M = P.mf;
         const float inv_dist = rsqrtf(d2);
         const float dist = d2 * inv_dist;
@@ -255,11 +263,9 @@ struct ForceAcc {
             const float rn2 = rn * rn, rn4 = rn2 * rn2, rn8 = rn4 * rn4;
             m -= M.lj_D * (rn8 * rn4 - rn4) * (inv_dist * inv_dist);
         }
-        const float4 vi = G.V4[i];
         const float rhoi = vi.w;
         const float sc = kernel_dwdr_scalef(intf_skf, M.kf[intf_skf], q, inv_dist, M.inv_h);
         if (intf) {
-            const float2 pri = G.PR[i];
             float pf = form1 ? __fdividef(prj.x + pri.x, rhoj * rhoi) : (pri.y + prj.y);
             if (P.art_pressure && (pri.x < 0 || prj.x < 0)) {
                 const float w = kernel_wf(P.ap_skf, M.kf[P.ap_skf], q);
@@ -449,7 +455,358 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_forces_mixed(DevParams P,
     }
 }
 
+// ------------------------------------------------------- neighbour reuse --
+// 2D FP32-mixed step with summation density. A particle's candidate list
+// holds the particles within cutoff + skin of it when the grid was last built;
+// while no particle has moved more than skin/2 since then, every pair within
+// the cutoff is in the lists, and each step tests the list instead of the 9
+// stencil cells (the pair set is the reference's: the same cutoff test). Each
+// particle's build cell stays its reference cell for the cell-relative
+// offsets until the next build.
+
+__global__ void k_vl_decide(cudaGraphConditionalHandle h, const uint32_t* __restrict__ rebuild) {
+    cudaGraphSetConditional(h, *rebuild ? 1u : 0u);
+}
+__global__ void k_vl_reset(uint32_t* __restrict__ rebuild, unsigned long long* __restrict__ builds) {
+    *rebuild = 0u;
+    *builds += 1ull;
+}
+
+// After this step's grid (sort + reorder): each particle's candidates, through
+// a per-thread list in shared memory ([kVerletCap][blockDim], conflict-free)
+// copied to the particle's row of the global list four entries per store. The
+// cell equals the cutoff, so a candidate within cutoff + skin can lie two
+// cells away: a particle within one skin of a cell edge also searches the
+// cells beyond that edge.
+__global__ void __launch_bounds__(kMaxGatherThreads) k_vl_build(DevParams P, State S, Sorted G) {
+    extern __shared__ uint32_t s_list[];
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= P.n) return;
+    const MixedF& M = P.mf;
+    const uint32_t id = G.id[k], key = G.key[k];
+    const float4 pj = G.P4[k];
+    const uint32_t cx = second_bits(key), cy = second_bits(key >> 1);
+    S.bcxy[id] = cx | (cy << 16);
+    S.boff[id] = make_float2(pj.x, pj.y);
+    const uint32_t bd = blockDim.x, t = threadIdx.x;
+    uint32_t nl = 0;
+    if (__float_as_int(pj.w) != P.type_non_existent) {
+        const float edge = P.vl_skin_edge;
+        const int x0 = (pj.x < edge && cx >= 2) ? -2 : (cx >= 1 ? -1 : 0);
+        const int x1 = (pj.x > M.cell - edge && cx + 2 <= kMaxCellCoord2) ? 2 : (cx + 1 <= kMaxCellCoord2 ? 1 : 0);
+        const int y0 = (pj.y < edge && cy >= 2) ? -2 : (cy >= 1 ? -1 : 0);
+        const int y1 = (pj.y > M.cell - edge && cy + 2 <= kMaxCellCoord2) ? 2 : (cy + 1 <= kMaxCellCoord2 ? 1 : 0);
+#pragma unroll 1
+        for (int dx = x0; dx <= x1; dx++) {
+#pragma unroll 1
+            for (int dy = y0; dy <= y1; dy++) {
+                const uint32_t cell = split2_32(cx + dx) | (split2_32(cy + dy) << 1);
+                if (cell >= P.max_cells) continue;
+                const uint32_t s = G.cell_start[cell];
+                if (s == kEmpty) continue;
+                const uint32_t e = G.cell_end[cell];
+                const float shx = (float)dx * M.cell - pj.x;
+                const float shy = (float)dy * M.cell - pj.y;
+                const uint32_t code = (uint32_t)((dx + 2) * 5 + (dy + 2)) << 27;
+                for (uint32_t i = s; i < e; i++) {
+                    if (i == k) continue;
+                    const float4 pi = G.P4[i];
+                    if (__float_as_int(pi.w) == P.type_non_existent) continue;  // stays non-existent
+                    const float ddx = pi.x + shx, ddy = pi.y + shy;
+                    if (ddx * ddx + ddy * ddy < P.vl_cut2) {
+                        if (nl < (uint32_t)kVerletCap) s_list[nl * bd + t] = i | code;
+                        nl++;
+                    }
+                }
+            }
+        }
+    }
+    const uint32_t m = nl < (uint32_t)kVerletCap ? nl : (uint32_t)kVerletCap;
+    uint4* row = reinterpret_cast<uint4*>(G.vlist + (size_t)k * kVerletCap);  // 256-byte aligned rows
+    for (uint32_t e = 0; e < m; e += 4) {
+        uint4 w;
+        w.x = s_list[e * bd + t];
+        w.y = e + 1 < m ? s_list[(e + 1) * bd + t] : kVlNone;
+        w.z = e + 2 < m ? s_list[(e + 2) * bd + t] : kVlNone;
+        w.w = e + 3 < m ? s_list[(e + 3) * bd + t] : kVlNone;
+        row[e >> 2] = w;
+    }
+    G.vcount[k] = nl <= (uint32_t)kVerletCap ? nl : kListOver;
+    if (nl > (uint32_t)kVerletCap) atomicOr(S.vl_rebuild, 1u);  // its search needs a fresh grid each step
+}
+
+// Steps that reuse the lists: cell-order copies, positions relative to each
+// particle's build cell (the key pass left the current cell and offset).
+__global__ void k_vl_reorder(DevParams P, State S, Sorted G) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= P.n) return;
+    const uint32_t id = G.id[k], key = G.key[k];
+    const uint32_t now = S.cxy[id];
+    const float2 o = S.coff2[id];
+    const float ox = o.x + (float)((int)(now & 0xFFFFu) - (int)second_bits(key)) * P.mf.cell;
+    const float oy = o.y + (float)((int)(now >> 16) - (int)second_bits(key >> 1)) * P.mf.cell;
+    G.P4[k] = make_float4(ox, oy, 0.0f, __int_as_float(S.itype[id]));
+    const float2 v = S.vpf2[id];
+    G.V4[k] = make_float4(v.x, v.y, 0.0f, 0.0f);  // .w: the density pass writes it
+}
+
+// density_sum (Density.h:25-61) + EOS over the candidate list: the entries
+// within the cutoff are this step's neighbours (recorded in vmask for the
+// force pass). A particle whose list overflowed searches the stencil cells
+// (the grid is rebuilt every step while one does).
+template <int SKF>
+__global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams P, State S, Sorted G,
+                                                                     StepScalars* __restrict__ scal,
+                                                                     uint32_t* __restrict__ flags) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = k < P.n;
+    uint32_t cnt = 0;
+    if (active) {
+        const MixedF& M = P.mf;
+        const uint32_t id = G.id[k];
+        const float4 pj = G.P4[k];
+        const int32_t tj = __float_as_int(pj.w);
+        const int skf = SKF ? SKF : P.density_skf;
+        const float f = M.kf[skf];
+        Kahan acc{0.0f, 0.0f};
+        unsigned long long mask = 0ull;
+        if (tj != P.type_non_existent) {
+            const uint32_t vc = G.vcount[k];
+            if (vc != kListOver) {
+                const uint4* row = reinterpret_cast<const uint4*>(G.vlist + (size_t)k * kVerletCap);
+                int cur = -1;
+                float shx = 0.0f, shy = 0.0f, part = 0.0f;
+                // groups of four entries (one load), then their particles, loaded together
+                for (uint32_t e0 = 0; e0 < vc; e0 += kVlBatch) {
+                    const uint4 w = row[e0 >> 2];
+                    const uint32_t en[kVlBatch] = {w.x, w.y, w.z, w.w};
+                    float4 pb[kVlBatch];
+#pragma unroll
+                    for (int j = 0; j < kVlBatch; j++)
+                        pb[j] = en[j] != kVlNone ? G.P4[en[j] & 0x07FFFFFFu] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+                    for (int j = 0; j < kVlBatch; j++) {
+                        if (en[j] == kVlNone) break;
+                        const int c = (int)(en[j] >> 27);
+                        if (c != cur) {
+                            if (cur >= 0) acc.add(M.mass * part);
+                            part = 0.0f;
+                            cur = c;
+                            shx = (float)(c / 5 - 2) * M.cell - pj.x;
+                            shy = (float)(c % 5 - 2) * M.cell - pj.y;
+                        }
+                        if (__float_as_int(pb[j].w) == P.type_non_existent) continue;
+                        const float dx = pb[j].x + shx, dy = pb[j].y + shy;
+                        const float d2 = dx * dx + dy * dy;
+                        if (!within_cutoff<2>(P, S, G, en[j] & 0x07FFFFFFu, k, d2)) continue;
+                        cnt++;
+                        mask |= 1ull << (e0 + j);
+                        part += kernel_wf(skf, f, d2 * rsqrtf(d2) * M.inv_h);
+                    }
+                }
+                if (cur >= 0) acc.add(M.mass * part);
+            } else {
+                const Stencil<2> st(P, G.key[k]);
+#pragma unroll 1
+                for (int c = 0; c < 9; c++) {
+                    uint32_t cell;
+                    int sx, sy, sz;
+                    if (!st.cell(c, cell, sx, sy, sz)) continue;
+                    const uint32_t s = G.cell_start[cell];
+                    if (s == kEmpty) continue;
+                    const uint32_t e = G.cell_end[cell];
+                    const float shx = (float)sx * M.cell - pj.x;
+                    const float shy = (float)sy * M.cell - pj.y;
+                    float part = 0.0f;
+                    for (uint32_t i = s; i < e; i++) {
+                        if (i == k) continue;
+                        const float4 pi = G.P4[i];
+                        if (__float_as_int(pi.w) == P.type_non_existent) continue;
+                        const float dx = pi.x + shx, dy = pi.y + shy;
+                        const float d2 = dx * dx + dy * dy;
+                        if (!within_cutoff<2>(P, S, G, i, k, d2)) continue;
+                        cnt++;
+                        part += kernel_wf(skf, f, d2 * rsqrtf(d2) * M.inv_h);
+                    }
+                    acc.add(M.mass * part);
+                }
+            }
+        }
+        G.vmask[k] = mask;
+        if (cnt > P.max_nb - 1) atomicOr(flags, RRSPH_FLAG_NEIGHBOUR_OVERFLOW);
+        const float d = ((acc.s - M.rho0_minus_w0_hi) - acc.c) - M.rho0_minus_w0_lo;
+        const float rho = M.rho0 + d;
+        const float pr = eos_pf(M, d);
+        G.V4[k].w = rho;
+        G.PR[k] = make_float2(pr, pr * __frcp_rn(rho * rho));
+        S.rho[id] = P.rho0 + f2d(d);
+        S.p[id] = f2d(pr);
+    }
+    warp_sum_add(&scal->pairs, cnt);
+}
+
+// update_acceleration over this step's neighbours: the list entries the
+// density pass marked (or the stencil search for an overflowed list).
+template <int SKF>
+__global__ void __launch_bounds__(kMaxGatherThreads) k_forces_verlet(DevParams P, State S, Sorted G,
+                                                                    StepScalars* __restrict__ scal,
+                                                                    uint32_t* __restrict__ flags) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = k < P.n;
+    double amag = 0, arvmu_d = 0;
+    if (active) {
+        const MixedF& M = P.mf;
+        const uint32_t id = G.id[k];
+        const float4 pj4 = G.P4[k];
+        const int32_t tj = __float_as_int(pj4.w);
+        ForceAcc<2, SKF> F{P, G, G.V4[k], G.PR[k], 0.0f, false, false, false, false, false, 0, 0,
+                           0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        F.rhoj = F.vj.w;
+        F.ext = P.repulsive && tj > 0;
+        F.intf = true;
+        F.visc = P.art_visc;
+        F.avel = P.avg_vel;
+        F.form1 = P.intf_form == 1;
+        F.intf_skf = SKF ? SKF : P.intf_skf;
+        F.av_skf = SKF ? SKF : P.av_skf;
+        Kahan ax{0, 0}, ay{0, 0};
+        Kahan avx{0, 0}, avy{0, 0};
+        if (tj != P.type_non_existent) {
+            const uint32_t vc = G.vcount[k];
+            if (vc != kListOver) {
+                const uint32_t* row = G.vlist + (size_t)k * kVerletCap;
+                unsigned long long left = G.vmask[k];
+                int cur = -1;
+                float shx = 0.0f, shy = 0.0f;
+                while (left) {
+                    // the next neighbours' list words (this particle's row, cached),
+                    // then their data, loaded together so that the loads overlap
+                    uint32_t en[kVlForceBatch];
+                    float4 pb[kVlForceBatch], vb[kVlForceBatch];
+                    float2 rb[kVlForceBatch];
+#pragma unroll
+                    for (int j = 0; j < kVlForceBatch; j++) {
+                        if (left) {
+                            en[j] = row[__ffsll((long long)left) - 1];
+                            left &= left - 1;
+                        } else {
+                            en[j] = kVlNone;
+                        }
+                    }
+#pragma unroll
+                    for (int j = 0; j < kVlForceBatch; j++) {
+                        if (en[j] == kVlNone) continue;
+                        const uint32_t i = en[j] & 0x07FFFFFFu;
+                        pb[j] = G.P4[i];
+                        vb[j] = G.V4[i];
+                        rb[j] = G.PR[i];
+                    }
+#pragma unroll
+                    for (int j = 0; j < kVlForceBatch; j++) {
+                        if (en[j] == kVlNone) continue;
+                        const int c = (int)(en[j] >> 27);
+                        if (c != cur) {
+                            if (cur >= 0) {
+                                ax.add(F.cax);
+                                ay.add(F.cay);
+                                if (F.avel) {
+                                    avx.add(F.cvx);
+                                    avy.add(F.cvy);
+                                }
+                            }
+                            F.cax = F.cay = F.cvx = F.cvy = 0.0f;
+                            cur = c;
+                            shx = (float)(c / 5 - 2) * M.cell - pj4.x;
+                            shy = (float)(c % 5 - 2) * M.cell - pj4.y;
+                        }
+                        const float dx = pb[j].x + shx, dy = pb[j].y + shy;
+                        F.pair_with(vb[j], rb[j], dx, dy, 0.0f, dx * dx + dy * dy, __float_as_int(pb[j].w));
+                    }
+                }
+                if (cur >= 0) {
+                    ax.add(F.cax);
+                    ay.add(F.cay);
+                    if (F.avel) {
+                        avx.add(F.cvx);
+                        avy.add(F.cvy);
+                    }
+                }
+            } else {
+                const Stencil<2> st(P, G.key[k]);
+#pragma unroll 1
+                for (int c = 0; c < 9; c++) {
+                    uint32_t cell;
+                    int sx, sy, sz;
+                    if (!st.cell(c, cell, sx, sy, sz)) continue;
+                    const uint32_t s = G.cell_start[cell];
+                    if (s == kEmpty) continue;
+                    const uint32_t e = G.cell_end[cell];
+                    const float shx = (float)sx * M.cell - pj4.x;
+                    const float shy = (float)sy * M.cell - pj4.y;
+                    F.cax = F.cay = F.cvx = F.cvy = 0.0f;
+                    for (uint32_t i = s; i < e; i++) {
+                        if (i == k) continue;
+                        const float4 pi4 = G.P4[i];
+                        const int32_t ti = __float_as_int(pi4.w);
+                        if (ti == P.type_non_existent) continue;
+                        const float dx = pi4.x + shx, dy = pi4.y + shy;
+                        const float d2 = dx * dx + dy * dy;
+                        if (!within_cutoff<2>(P, S, G, i, k, d2)) continue;
+                        F.pair(i, dx, dy, 0.0f, d2, ti);
+                    }
+                    ax.add(F.cax);
+                    ay.add(F.cay);
+                    if (F.avel) {
+                        avx.add(F.cvx);
+                        avy.add(F.cvy);
+                    }
+                }
+            }
+        }
+        const double axd = ax.value(), ayd = ay.value() - P.g;
+        S.ax[id] = axd;
+        S.ay[id] = ayd;
+        if (F.avel) {
+            S.avx[id] = avx.value();
+            S.avy[id] = avy.value();
+        }
+        arvmu_d = F.arvmu;
+        if (P.dt_reduce) amag = sqrt(axd * axd + ayd * ayd);
+    }
+    if (P.dt_method == 2 && P.dt_reduce) {
+        warp_max_bits(&scal->amax_bits, amag);
+        warp_max_bits(&scal->mumax_bits, arvmu_d);
+    }
+}
+
 }  // namespace
+
+void launch_verlet_decide(cudaGraphConditionalHandle h, const uint32_t* rebuild, cudaStream_t st) {
+    k_vl_decide<<<1, 1, 0, st>>>(h, rebuild);
+}
+void launch_verlet_reset(uint32_t* rebuild, unsigned long long* builds, cudaStream_t st) {
+    k_vl_reset<<<1, 1, 0, st>>>(rebuild, builds);
+}
+void launch_verlet_build(const DevParams& P, const State& S, const Sorted& G, cudaStream_t st) {
+    constexpr int kBuildThreads = 128;  // the per-thread lists take 32 KB of shared memory
+    const size_t smem = (size_t)kVerletCap * kBuildThreads * sizeof(uint32_t);
+    k_vl_build<<<(P.n + kBuildThreads - 1) / kBuildThreads, kBuildThreads, smem, st>>>(P, S, G);
+}
+void launch_verlet_reorder(const DevParams& P, const State& S, const Sorted& G, cudaStream_t st) {
+    k_vl_reorder<<<(P.n + 255) / 256, 256, 0, st>>>(P, S, G);
+}
+void launch_density_verlet(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
+                           cudaStream_t st, int threads) {
+    const unsigned blocks = (P.n + threads - 1) / threads;
+    if (P.all_cubic) k_density_verlet<1><<<blocks, threads, 0, st>>>(P, S, G, scal, flags);
+    else k_density_verlet<0><<<blocks, threads, 0, st>>>(P, S, G, scal, flags);
+}
+void launch_forces_verlet(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
+                          cudaStream_t st, int threads) {
+    const unsigned blocks = (P.n + threads - 1) / threads;
+    if (P.all_cubic) k_forces_verlet<1><<<blocks, threads, 0, st>>>(P, S, G, scal, flags);
+    else k_forces_verlet<0><<<blocks, threads, 0, st>>>(P, S, G, scal, flags);
+}
 
 template <int DIM>
 void launch_density_mixed(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,

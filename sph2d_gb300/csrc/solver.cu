@@ -176,6 +176,27 @@ int key_bits(uint64_t max_cells) {
     return b < 1 ? 1 : b;
 }
 
+void drop_graphs(rrsph_solver* s) {
+    cudaStreamSynchronize(s->stream);
+    for (auto& g : s->graph) {
+        if (g) cudaGraphExecDestroy(g);
+        g = nullptr;
+    }
+}
+
+// Candidate-list cutoff (cell + skin, widened a little: a list may hold more
+// than the pairs within it, never fewer), (skin / 2)^2 slightly narrowed, the
+// edge band that looks two cells away, and the launches a rebuild adds.
+void set_verlet_params(rrsph_solver* s) {
+    const double skin = s->verlet_skin * s->params.hsml;
+    const double c = s->P.cell + skin;
+    s->P.vl_cut2 = (float)(c * c * (1.0 + 1e-4));
+    s->P.vl_half_skin2 = (float)(0.25 * skin * skin * (1.0 - 1e-4));
+    s->P.vl_skin_edge = (float)(skin * 1.01);
+    // reset + sort (3 per 8-bit pass) + reorder + build, against the reuse copy's 1
+    s->vl_extra_launches = 2ull + 3ull * (unsigned long long)((s->sort_bits + 7) / 8);
+}
+
 int check_handle(rrsph_solver* s, const char* fn) {
     if (!s) return set_error(RRSPH_ERR_INVALID_ARGUMENT, std::string(fn) + ": null solver");
     cudaError_t e = cudaSetDevice(s->device);
@@ -215,6 +236,109 @@ void enqueue_forces(rrsph_solver* s, uint32_t terms, rrsph::StepScalars* scal, i
 // phases. with_keys runs the predict + key pass first; otherwise the previous
 // step's whole-step kernel has done it. The whole-step kernel always prepares
 // the next step's predict + keys.
+// Neighbour reuse: the grid + list rebuild, or the cell-order copies of a
+// step that reuses the lists, on stream st. The rebuilt grid stays in
+// (keys_a, ids_a) while the lists are reused: the key pass of every step
+// rewrites keys_in.
+void enqueue_verlet_rebuild(rrsph_solver* s, cudaStream_t st) {
+    rrsph::launch_verlet_reset(s->S.vl_rebuild, s->vl_builds, st);
+    rrsph::radix_sort_pairs_into(s->G.keys_in, s->G.ids_in, s->G.keys_a, s->G.ids_a, s->G.keys_b, s->G.ids_b,
+                                 s->G.sort_scratch, s->P.n, s->sort_bits, st, &s->launches);
+    s->G.key = s->G.keys_a;
+    s->G.id = s->G.ids_a;
+    rrsph::GatherSrc fsrc{s->S.vpx, s->S.vpy, s->S.vpz, s->S.rho, nullptr, 1};
+    rrsph::launch_reorder<2>(s->P, s->S, s->G, fsrc, 1, st);
+    rrsph::launch_verlet_build(s->P, s->S, s->G, st);
+    s->launches += 3;
+}
+void enqueue_verlet_reuse(rrsph_solver* s, cudaStream_t st) {
+    rrsph::launch_verlet_reorder(s->P, s->S, s->G, st);
+    s->launches++;
+}
+
+// One step of the 2D mixed loop with neighbour reuse. In a captured graph the
+// rebuild / reuse choice is a conditional node that a kernel sets from the flag
+// the last key pass raised; with direct launches the host reads the flag.
+int enqueue_step_verlet(rrsph_solver* s, int par, cudaEvent_t* events, bool with_keys) {
+    rrsph::StepScalars* cur = s->scal + par;
+    rrsph::StepScalars* nxt = s->scal + (par ^ 1);
+    cudaStream_t st = s->stream;
+    s->G.key = s->G.keys_a;  // the grid of the last rebuild
+    s->G.id = s->G.ids_a;
+    if (events) cudaEventRecord(events[0], st);
+    if (with_keys) {
+        rrsph::launch_keys<2>(s->P, s->S, s->G, cur, 1, s->flags, st);
+        s->launches++;
+    }
+    if (events) cudaEventRecord(events[1], st);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    RRSPH_CUDA_TRY(cudaStreamIsCapturing(st, &cs));
+    if (cs == cudaStreamCaptureStatusActive) {
+        cudaGraph_t g = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        RRSPH_CUDA_TRY(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd));
+        cudaGraphConditionalHandle h;
+        RRSPH_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+        rrsph::launch_verlet_decide(h, s->S.vl_rebuild, st);
+        s->launches++;
+        RRSPH_CUDA_TRY(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd));
+        cudaGraphNodeParams np{};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeIf;
+        np.conditional.size = 2;
+        cudaGraphNode_t cnode;
+        RRSPH_CUDA_TRY(cudaGraphAddNode(&cnode, g, deps, nullptr, nd, &np));
+        s->vl_body[0] = np.conditional.phGraph_out[0];
+        s->vl_body[1] = np.conditional.phGraph_out[1];
+        s->vl_pending = true;
+        RRSPH_CUDA_TRY(cudaStreamUpdateCaptureDependencies(st, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+    } else {
+        RRSPH_CUDA_TRY(cudaMemcpyAsync(s->h_vl, s->S.vl_rebuild, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
+        if (*s->h_vl) {
+            const unsigned long long before = s->launches;
+            enqueue_verlet_rebuild(s, st);
+            s->launches = before + 1;  // a rebuild's extra launches are counted from vl_builds
+        } else {
+            enqueue_verlet_reuse(s, st);
+        }
+    }
+    if (events) {
+        cudaEventRecord(events[2], st);
+        cudaEventRecord(events[3], st);
+    }
+    rrsph::launch_density_verlet(s->P, s->S, s->G, cur, s->flags, st, s->gather_threads[0]);
+    if (events) cudaEventRecord(events[4], st);
+    rrsph::launch_forces_verlet(s->P, s->S, s->G, cur, s->flags, st, s->gather_threads[1]);
+    if (events) cudaEventRecord(events[5], st);
+    rrsph::launch_whole_step<2>(s->P, s->S, s->G, cur, nxt, s->flags, 1, st);
+    if (events) cudaEventRecord(events[6], st);
+    s->launches += 3;
+    return RRSPH_OK;
+}
+
+// Fills the bodies of the conditional node of a just-captured reuse step;
+// *reuse_launches gets the launches of the reuse body.
+int capture_verlet_bodies(rrsph_solver* s, unsigned long long* reuse_launches) {
+    s->vl_pending = false;
+    unsigned long long counts[2] = {0, 0};
+    for (int b = 0; b < 2; b++) {
+        const unsigned long long before = s->launches;
+        RRSPH_CUDA_TRY(cudaStreamBeginCaptureToGraph(s->aux, s->vl_body[b], nullptr, nullptr, 0,
+                                                     cudaStreamCaptureModeThreadLocal));
+        if (b == 0) enqueue_verlet_rebuild(s, s->aux);
+        else enqueue_verlet_reuse(s, s->aux);
+        cudaGraph_t out = nullptr;
+        RRSPH_CUDA_TRY(cudaStreamEndCapture(s->aux, &out));
+        counts[b] = s->launches - before;
+        s->launches = before;
+    }
+    *reuse_launches = counts[1];
+    return RRSPH_OK;
+}
+
 template <int DIM>
 void enqueue_step(rrsph_solver* s, int par, cudaEvent_t* events, bool with_keys) {
     rrsph::StepScalars* cur = s->scal + par;
@@ -241,9 +365,11 @@ void enqueue_step(rrsph_solver* s, int par, cudaEvent_t* events, bool with_keys)
     s->launches += 2;
 }
 
-void enqueue_step_dim(rrsph_solver* s, int par, cudaEvent_t* events, bool with_keys) {
+int enqueue_step_dim(rrsph_solver* s, int par, cudaEvent_t* events, bool with_keys) {
+    if (s->verlet) return enqueue_step_verlet(s, par, events, with_keys);
     if (s->dim == 3) enqueue_step<3>(s, par, events, with_keys);
     else enqueue_step<2>(s, par, events, with_keys);
+    return RRSPH_OK;
 }
 
 void enqueue_keys_dim(rrsph_solver* s, int par) {
@@ -338,6 +464,11 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
         if (cont) { A(G.vdx, n); A(G.vdy, n); if (d3) A(G.vdz, n); A(G.rhod, n); }
     } else {
         if (d3) { A(S.coff4, n); A(S.vpf4, n); } else { A(S.coff2, n); A(S.vpf2, n); }
+        if (!d3 && !cont) {  // neighbour reuse
+            A(S.cxy, n); A(S.bcxy, n); A(S.boff, n); A(S.vl_rebuild, 1); A(s->vl_builds, 1);
+            A(G.vlist, (size_t)rrsph::kVerletCap * n); A(G.vcount, n); A(G.vmask, n);
+            A(G.keys_b, n); A(G.ids_b, n);
+        }
         A(G.P4, n); A(G.V4, n); A(G.PR, n);
         if (!d3) A(G.nbmask, 10 * n);
         if (cont) A(G.VD4, n);
@@ -345,6 +476,23 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
     A(s->scal, 2);
     A(s->flags, 1);
 #undef A
+    if (S.vl_rebuild) {
+        if (cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaMallocHost(&s->h_vl, sizeof(uint32_t)) != cudaSuccess)
+            return fail(set_error(RRSPH_ERR_CUDA, "rrsph_create: neighbour-reuse stream"));
+        // no lists yet: empty lists, masks and grid until the first build (which the flag forces)
+        if (cudaMemsetAsync(S.vl_rebuild, 0xFF, sizeof(uint32_t), s->stream) != cudaSuccess ||
+            cudaMemsetAsync(s->vl_builds, 0, sizeof(unsigned long long), s->stream) != cudaSuccess ||
+            cudaMemsetAsync(G.vcount, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
+            cudaMemsetAsync(G.vmask, 0, n * sizeof(unsigned long long), s->stream) != cudaSuccess ||
+            cudaMemsetAsync(S.bcxy, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
+            cudaMemsetAsync(S.boff, 0, n * sizeof(float2), s->stream) != cudaSuccess ||
+            cudaMemsetAsync(G.keys_a, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
+            cudaMemsetAsync(G.ids_a, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess)
+            return fail(set_error(RRSPH_ERR_CUDA, "rrsph_create: memset failed"));
+        s->verlet = true;
+        set_verlet_params(s);
+    }
     if (cudaMallocHost(&s->h_scal, sizeof(rrsph::StepScalars)) != cudaSuccess ||
         cudaMallocHost(&s->h_flags, sizeof(uint32_t)) != cudaSuccess ||
         cudaMallocHost(&s->h_time, sizeof(double)) != cudaSuccess)
@@ -378,6 +526,8 @@ extern "C" void rrsph_destroy(rrsph_solver* s) {
     if (s->h_scal) cudaFreeHost(s->h_scal);
     if (s->h_flags) cudaFreeHost(s->h_flags);
     if (s->h_time) cudaFreeHost(s->h_time);
+    if (s->h_vl) cudaFreeHost(s->h_vl);
+    if (s->aux) cudaStreamDestroy(s->aux);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
 }
@@ -421,6 +571,7 @@ extern "C" int rrsph_upload(rrsph_solver* s, const double* r, uint32_t stride, c
     init.dt = s->params.dt;
     std::memcpy(s->h_scal, &init, sizeof(init));
     RRSPH_CUDA_TRY(cudaMemcpyAsync(s->scal, s->h_scal, sizeof(init), cudaMemcpyHostToDevice, st));
+    if (S.vl_rebuild) RRSPH_CUDA_TRY(cudaMemsetAsync(S.vl_rebuild, 0xFF, sizeof(uint32_t), st));
     RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
     s->step_index = 0;
     s->keys_ready = false;
@@ -458,7 +609,8 @@ int enqueue_steps(rrsph_solver* s, uint64_t nsteps) {
         const bool with_keys = !s->keys_ready;
         s->keys_ready = true;
         if (s->timing) {
-            enqueue_step_dim(s, par, s->ev, with_keys);
+            int rc = enqueue_step_dim(s, par, s->ev, with_keys);
+            if (rc) return rc;
             RRSPH_CUDA_TRY(cudaEventSynchronize(s->ev[kPhases]));
             for (int i = 0; i < kPhases; i++) {
                 float ms = 0;
@@ -471,19 +623,34 @@ int enqueue_steps(rrsph_solver* s, uint64_t nsteps) {
                 cudaGraph_t g = nullptr;
                 const unsigned long long before = s->launches;
                 RRSPH_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-                enqueue_step_dim(s, par, nullptr, false);
-                RRSPH_CUDA_TRY(cudaStreamEndCapture(st, &g));
+                const int rc = enqueue_step_dim(s, par, nullptr, false);
+                const cudaError_t ce = cudaStreamEndCapture(st, &g);
+                if (rc) {
+                    if (g) cudaGraphDestroy(g);
+                    return rc;
+                }
+                if (ce != cudaSuccess)
+                    return set_error(RRSPH_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ce));
+                unsigned long long body = 0;
+                if (s->vl_pending) {
+                    const int rb = capture_verlet_bodies(s, &body);
+                    if (rb) {
+                        cudaGraphDestroy(g);
+                        return rb;
+                    }
+                }
                 const cudaError_t e = cudaGraphInstantiate(&s->graph[par], g, 0);
                 cudaGraphDestroy(g);
                 if (e != cudaSuccess) return set_error(RRSPH_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
-                s->launches_in_graph[par] = s->launches - before;
+                s->launches_in_graph[par] = s->launches - before + body;
                 s->launches = before;
             }
             if (with_keys) enqueue_keys_dim(s, par);
             RRSPH_CUDA_TRY(cudaGraphLaunch(s->graph[par], st));
             s->launches += s->launches_in_graph[par];
         } else {
-            enqueue_step_dim(s, par, nullptr, with_keys);
+            int rc = enqueue_step_dim(s, par, nullptr, with_keys);
+            if (rc) return rc;
         }
         s->step_index++;
     }
@@ -577,6 +744,7 @@ namespace {
 template <int DIM>
 void enqueue_component_grid(rrsph_solver* s, bool with_p) {
     s->keys_ready = false;  // this grid's keys were made without the predictor
+    if (s->S.vl_rebuild) cudaMemsetAsync(s->S.vl_rebuild, 0xFF, sizeof(uint32_t), s->stream);
     rrsph::GatherSrc fsrc{s->S.vx, s->S.vy, s->S.vz, s->S.rho, with_p ? s->S.p : nullptr, 0};
     enqueue_grid<DIM>(s, 0, s->scal, fsrc);
 }
@@ -716,7 +884,43 @@ extern "C" int rrsph_phase_times(rrsph_solver* s, double* ms_per_phase, int coun
 }
 extern "C" int rrsph_kernel_launches(rrsph_solver* s, uint64_t* launches) {
     if (!s || !launches) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_kernel_launches: null argument");
-    *launches = s->launches;
+    uint64_t builds = 0;
+    if (s->vl_builds) {  // a step counts its reuse branch; add what each rebuild launched on top
+        int rc = rrsph_neighbour_rebuilds(s, &builds);
+        if (rc) return rc;
+    }
+    *launches = s->launches + builds * s->vl_extra_launches;
+    return RRSPH_OK;
+}
+
+extern "C" int rrsph_neighbour_rebuilds(rrsph_solver* s, uint64_t* rebuilds) {
+    int rc = check_handle(s, "rrsph_neighbour_rebuilds");
+    if (rc) return rc;
+    if (!rebuilds) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_neighbour_rebuilds: null argument");
+    *rebuilds = 0;
+    if (!s->vl_builds) return RRSPH_OK;
+    unsigned long long v = 0;
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(&v, s->vl_builds, sizeof(v), cudaMemcpyDeviceToHost, s->stream));
+    RRSPH_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    *rebuilds = v;
+    return RRSPH_OK;
+}
+
+extern "C" int rrsph_set_neighbour_reuse(rrsph_solver* s, int enable, double skin_over_h) {
+    int rc = check_handle(s, "rrsph_set_neighbour_reuse");
+    if (rc) return rc;
+    if (enable && !s->S.vl_rebuild)
+        return set_error(RRSPH_ERR_UNSUPPORTED, "neighbour reuse needs a 2D FP32-mixed solver with summation density");
+    if (enable && !(skin_over_h > 0 && skin_over_h <= 1))
+        return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_set_neighbour_reuse: skin must be in (0, 1] hsml");
+    drop_graphs(s);
+    s->verlet = enable != 0;
+    if (enable) {
+        s->verlet_skin = skin_over_h;
+        set_verlet_params(s);
+    }
+    if (s->S.vl_rebuild) RRSPH_CUDA_TRY(cudaMemsetAsync(s->S.vl_rebuild, 0xFF, sizeof(uint32_t), s->stream));
+    s->keys_ready = false;
     return RRSPH_OK;
 }
 
@@ -724,13 +928,6 @@ extern "C" int rrsph_kernel_launches(rrsph_solver* s, uint64_t* launches) {
 
 namespace {
 
-void drop_graphs(rrsph_solver* s) {
-    cudaStreamSynchronize(s->stream);
-    for (auto& g : s->graph) {
-        if (g) cudaGraphExecDestroy(g);
-        g = nullptr;
-    }
-}
 
 // A device copy of the particle state and step scalars (the autotuner runs
 // trial steps on the uploaded state and puts it back).
@@ -770,6 +967,7 @@ int restore_state(rrsph_solver* s, const Backup& b) {
         src += f.second;
     }
     RRSPH_CUDA_TRY(cudaMemcpyAsync(s->scal, b.scal, sizeof(b.scal), cudaMemcpyHostToDevice, s->stream));
+    if (s->S.vl_rebuild) RRSPH_CUDA_TRY(cudaMemsetAsync(s->S.vl_rebuild, 0xFF, sizeof(uint32_t), s->stream));
     RRSPH_CUDA_TRY(cudaStreamSynchronize(s->stream));
     s->step_index = b.step_index;
     s->keys_ready = false;

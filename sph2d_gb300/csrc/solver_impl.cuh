@@ -49,6 +49,15 @@ struct rrsph_solver {
     uint64_t timed_steps = 0;
     rrsph_impl::AdjointRun* adj = nullptr;
     int gather_threads[2] = {rrsph::kGatherThreads, rrsph::kGatherThreads};  // density, forces block sizes
+    // neighbour reuse of the 2D FP32-mixed step (summation density)
+    bool verlet = false;
+    double verlet_skin = 0.3;                  // skin, in units of hsml
+    cudaStream_t aux = nullptr;                // captures the rebuild / reuse bodies of a step graph
+    unsigned long long* vl_builds = nullptr;   // device: list builds since creation
+    uint32_t* h_vl = nullptr;                  // pinned: the rebuild flag, read with direct launches
+    cudaGraph_t vl_body[2] = {nullptr, nullptr};  // bodies of the graph being captured (rebuild, reuse)
+    bool vl_pending = false;
+    unsigned long long vl_extra_launches = 0;  // launches a rebuild adds to a reuse step
 };
 
 namespace rrsph_impl {

@@ -230,6 +230,15 @@ class Solver:
         check(lib().rrsph_autotune(self._h, steps, out))
         return int(out[0]), int(out[1])
 
+    def set_neighbour_reuse(self, enable: bool, skin_over_h: float = 0.3) -> None:
+        """Candidate-list reuse of the 2D mixed step (summation density)."""
+        check(lib().rrsph_set_neighbour_reuse(self._h, 1 if enable else 0, float(skin_over_h)))
+
+    def neighbour_rebuilds(self) -> int:
+        v = C.c_uint64()
+        check(lib().rrsph_neighbour_rebuilds(self._h, C.byref(v)))
+        return int(v.value)
+
     # -- piston optimisation
     def set_piston_fourier(self, omega: float, coef) -> None:
         """Piston displacement X(t) = sum_k coef[k-1] sin(k omega t) (empty coef: the wave maker's own law)."""

@@ -489,3 +489,47 @@ def test_cell_keys_at_cell_edges(gpu_available, precision):
     ref_keys, ref_grid, _ = O.grid(p, r)
     assert np.array_equal(keys, ref_keys)
     assert np.array_equal(grid, ref_grid)
+
+
+def test_neighbour_reuse_keeps_the_pairs_and_the_step(gpu_available):
+    """The 2D mixed step with candidate-list reuse (the default) against the
+    same step searching every step: identical pair counts every step, the
+    state within float rounding, and far fewer grid rebuilds than steps."""
+    from sph2d_gb300 import Solver
+
+    case = _dam(nx=60, ny=30)
+    p = case.params()
+    out = []
+    for reuse in (True, False):
+        with Solver(p, "mixed") as s:
+            s.set_neighbour_reuse(reuse)
+            s.upload(case.r, case.v, case.rho, case.itype)
+            pairs = []
+            t = 0.0
+            for _ in range(40):
+                t = s.step(1, t)
+                pairs.append(s.pair_count()[0])
+            out.append((s.download(), pairs, s.neighbour_rebuilds()))
+    (a, pa, ra), (b, pb, rb) = out
+    assert pa == pb
+    assert rb == 0 and 1 <= ra < 40
+    for k in ("r", "v", "rho"):
+        assert rel_l2(a[k], b[k]) < 1e-5, k
+
+
+def test_neighbour_reuse_graph_and_direct_launches_agree(gpu_available):
+    from sph2d_gb300 import Solver
+
+    case = _dam(nx=60, ny=30)
+    p = case.params()
+    out = []
+    for timing in (False, True):
+        with Solver(p, "mixed") as s:
+            s.set_phase_timing(timing)
+            s.upload(case.r, case.v, case.rho, case.itype)
+            s.step(25, 0.0)
+            out.append((s.download(), s.neighbour_rebuilds(), s.kernel_launches()))
+    assert out[0][1] == out[1][1]
+    assert out[0][2] == out[1][2] + 25  # a graph step also launches the kernel that picks its branch
+    for k in ("r", "v", "rho", "p"):
+        assert np.array_equal(out[0][0][k], out[1][0][k]), k
