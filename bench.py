@@ -40,11 +40,14 @@ METRIC = "pair-interactions/s and ms/step: FP32-mixed vs FP64 GPU step at stated
 UNIT = "pair-interactions/s"
 L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
 
-# Algorithmic bytes per particle of the dominant kernel (the force gather) of
-# the FP32-mixed 2D step: reads cell key 4, id 4, position+type float4 16,
-# velocity+density float4 16, (p, p/rho^2) float2 8, the 10 neighbour-mask words
-# the density pass wrote 40; writes a.x, a.y as double 16.
-FORCES_MIXED_BYTES_PER_PARTICLE = 100
+# Algorithmic bytes of the dominant kernel (the force gather, k_forces_verlet)
+# of the FP32-mixed 2D step with neighbour reuse: per particle it reads its id 4,
+# position+type float4 16, velocity+density float4 16, (p, p/rho^2) float2 8,
+# list count 4 and this step's neighbour mask 8, and writes a.x, a.y as double
+# 16; per neighbour pair it reads one 4-byte list word. The neighbours' own data
+# are re-reads of particles other threads load (L1/L2), not algorithmic bytes.
+FORCES_REUSE_BYTES_PER_PARTICLE = 4 + 16 + 16 + 8 + 4 + 8 + 16
+FORCES_REUSE_BYTES_PER_PAIR = 4
 FORCES_FP64_BYTES_PER_PARTICLE_2D = 4 + 4 + 16 + 4 + 16 + 8 + 8 + 16
 
 
@@ -58,6 +61,7 @@ def workload_config(case, p, pairs):
         "h": case.notes["h"],
         "dt": case.notes["dt"],
         "precision": "mixed (f32 pairs, f64 state/integration)",
+        "neighbour_search": "candidate lists within cutoff + 0.3 h, rebuilt when a particle has moved 0.15 h",
         "l2": "flushed (256 MiB device write) before every timed step",
         "parallelism": "replicas",
     }
@@ -185,6 +189,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     sm.sync()
     clocks = ClockSampler(local_rank)
     launches0 = sm.kernel_launches()
+    rebuilds0 = sm.neighbour_rebuilds()
     _, pairs0 = sm.pair_count()
     if dist:
         dist.barrier()
@@ -196,6 +201,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     if dist:
         dist.barrier()
     launches = sm.kernel_launches() - launches0
+    rebuilds = sm.neighbour_rebuilds() - rebuilds0
     last_pairs, pairs1 = sm.pair_count()
     pairs_timed = pairs1 - pairs0
     phases_mixed = _phase_pass(sm, flush, min(args.steps, 50))
@@ -272,7 +278,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
 
     fkey = "forces"
     f_ms = phases_mixed[fkey]
-    bytes_launch = FORCES_MIXED_BYTES_PER_PARTICLE * n
+    bytes_launch = FORCES_REUSE_BYTES_PER_PARTICLE * n + FORCES_REUSE_BYTES_PER_PAIR * last_pairs
     achieved = bytes_launch / (f_ms * 1e-3) / 1e9
     traffic = _profile_traffic()
     result = {
@@ -300,7 +306,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         "phases_ms_per_step": phases_mixed,
         "roofline": {
             "bound": "hbm",
-            "kernel": "k_forces_mixed",
+            "kernel": "k_forces_verlet",
             "achieved": achieved,
             "peak": hbm_peak,
             "unit": "GB/s",
@@ -313,6 +319,8 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": e2e_steps, "path": "rrsph_upload + rrsph_step(1) + rrsph_download, pinned host buffers"},
         "gpu_launches": launches,
+        "neighbour_rebuilds": {"timed_steps": args.steps, "rebuilds": rebuilds,
+                               "note": "grid + candidate lists rebuilt when a particle moved half the 0.3 h skin"},
         "clocks": clocks_info,
     }
     sm.close()
@@ -436,7 +444,7 @@ def adjoint_measure(steps: int = 500, checkpoint_every: int = 100) -> dict:
 
 def _profile_traffic():
     """DRAM bytes per launch of the force kernel from the committed ncu summary."""
-    f = ROOT / "profiles" / "forces_mixed_flume.txt"
+    f = ROOT / "profiles" / "forces_reuse_flume.txt"
     if not f.exists():
         return None
     for line in f.read_text().splitlines():

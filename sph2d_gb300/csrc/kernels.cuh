@@ -31,6 +31,7 @@ struct State {
     uint32_t* bcxy;            // cell coordinates at the last list build
     float2* boff;              // offset from that cell's edge at the last list build
     uint32_t* vl_rebuild;      // non-zero: the next step rebuilds the grid and the lists
+    uint32_t* vl_gone;         // the last build: bit 0 left out non-existent particles, bit 1 overflowed a list
 };
 
 // Per-step cell-ordered copies and the grid.
@@ -105,7 +106,10 @@ void launch_whole_step(const DevParams& P, const State& S, const Sorted& G, Step
 // are built with the cutoff widened by a skin and reused while no particle has
 // moved more than half the skin since the build (kernels_mixed.cu).
 void launch_verlet_decide(cudaGraphConditionalHandle h, const uint32_t* rebuild, cudaStream_t st);
-void launch_verlet_reset(uint32_t* rebuild, unsigned long long* builds, cudaStream_t st);
+void launch_verlet_reset(uint32_t* rebuild, uint32_t* gone, unsigned long long* builds, cudaStream_t st);
+// After an upload: the lists stay valid unless the last build left out a
+// non-existent particle (which may exist now); moves are checked by the key pass.
+void launch_verlet_upload_check(uint32_t* rebuild, const uint32_t* gone, cudaStream_t st);
 void launch_verlet_build(const DevParams& P, const State& S, const Sorted& G, cudaStream_t st);
 void launch_verlet_reorder(const DevParams& P, const State& S, const Sorted& G, cudaStream_t st);
 void launch_density_verlet(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,

@@ -467,9 +467,18 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_forces_mixed(DevParams P,
 __global__ void k_vl_decide(cudaGraphConditionalHandle h, const uint32_t* __restrict__ rebuild) {
     cudaGraphSetConditional(h, *rebuild ? 1u : 0u);
 }
-__global__ void k_vl_reset(uint32_t* __restrict__ rebuild, unsigned long long* __restrict__ builds) {
+__global__ void k_vl_reset(uint32_t* __restrict__ rebuild, uint32_t* __restrict__ gone,
+                           unsigned long long* __restrict__ builds) {
     *rebuild = 0u;
+    *gone = 0u;
     *builds += 1ull;
+}
+// After an upload: a flag raised by the key pass that ran for the replaced
+// positions is dropped (the next key pass checks the uploaded ones), unless no
+// list exists yet (all bits set) or the last build left out a non-existent
+// particle or overflowed a list.
+__global__ void k_vl_upload_check(uint32_t* __restrict__ rebuild, const uint32_t* __restrict__ gone) {
+    if (*rebuild != 0xFFFFFFFFu) *rebuild = *gone ? 1u : 0u;
 }
 
 // After this step's grid (sort + reorder): each particle's candidates, through
@@ -490,6 +499,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_vl_build(DevParams P, Sta
     S.boff[id] = make_float2(pj.x, pj.y);
     const uint32_t bd = blockDim.x, t = threadIdx.x;
     uint32_t nl = 0;
+    if (__float_as_int(pj.w) == P.type_non_existent) atomicOr(S.vl_gone, 1u);
     if (__float_as_int(pj.w) != P.type_non_existent) {
         const float edge = P.vl_skin_edge;
         const int x0 = (pj.x < edge && cx >= 2) ? -2 : (cx >= 1 ? -1 : 0);
@@ -532,7 +542,10 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_vl_build(DevParams P, Sta
         row[e >> 2] = w;
     }
     G.vcount[k] = nl <= (uint32_t)kVerletCap ? nl : kListOver;
-    if (nl > (uint32_t)kVerletCap) atomicOr(S.vl_rebuild, 1u);  // its search needs a fresh grid each step
+    if (nl > (uint32_t)kVerletCap) {  // its search needs a fresh grid each step
+        atomicOr(S.vl_rebuild, 1u);
+        atomicOr(S.vl_gone, 2u);
+    }
 }
 
 // Steps that reuse the lists: cell-order copies, positions relative to each
@@ -784,8 +797,11 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_forces_verlet(DevParams P
 void launch_verlet_decide(cudaGraphConditionalHandle h, const uint32_t* rebuild, cudaStream_t st) {
     k_vl_decide<<<1, 1, 0, st>>>(h, rebuild);
 }
-void launch_verlet_reset(uint32_t* rebuild, unsigned long long* builds, cudaStream_t st) {
-    k_vl_reset<<<1, 1, 0, st>>>(rebuild, builds);
+void launch_verlet_reset(uint32_t* rebuild, uint32_t* gone, unsigned long long* builds, cudaStream_t st) {
+    k_vl_reset<<<1, 1, 0, st>>>(rebuild, gone, builds);
+}
+void launch_verlet_upload_check(uint32_t* rebuild, const uint32_t* gone, cudaStream_t st) {
+    k_vl_upload_check<<<1, 1, 0, st>>>(rebuild, gone);
 }
 void launch_verlet_build(const DevParams& P, const State& S, const Sorted& G, cudaStream_t st) {
     constexpr int kBuildThreads = 128;  // the per-thread lists take 32 KB of shared memory

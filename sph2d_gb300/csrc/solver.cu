@@ -241,7 +241,7 @@ void enqueue_forces(rrsph_solver* s, uint32_t terms, rrsph::StepScalars* scal, i
 // (keys_a, ids_a) while the lists are reused: the key pass of every step
 // rewrites keys_in.
 void enqueue_verlet_rebuild(rrsph_solver* s, cudaStream_t st) {
-    rrsph::launch_verlet_reset(s->S.vl_rebuild, s->vl_builds, st);
+    rrsph::launch_verlet_reset(s->S.vl_rebuild, s->S.vl_gone, s->vl_builds, st);
     rrsph::radix_sort_pairs_into(s->G.keys_in, s->G.ids_in, s->G.keys_a, s->G.ids_a, s->G.keys_b, s->G.ids_b,
                                  s->G.sort_scratch, s->P.n, s->sort_bits, st, &s->launches);
     s->G.key = s->G.keys_a;
@@ -465,7 +465,8 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
     } else {
         if (d3) { A(S.coff4, n); A(S.vpf4, n); } else { A(S.coff2, n); A(S.vpf2, n); }
         if (!d3 && !cont) {  // neighbour reuse
-            A(S.cxy, n); A(S.bcxy, n); A(S.boff, n); A(S.vl_rebuild, 1); A(s->vl_builds, 1);
+            A(S.cxy, n); A(S.bcxy, n); A(S.boff, n); A(S.vl_rebuild, 2); A(s->vl_builds, 1);
+            S.vl_gone = S.vl_rebuild + 1;
             A(G.vlist, (size_t)rrsph::kVerletCap * n); A(G.vcount, n); A(G.vmask, n);
             A(G.keys_b, n); A(G.ids_b, n);
         }
@@ -482,6 +483,7 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
             return fail(set_error(RRSPH_ERR_CUDA, "rrsph_create: neighbour-reuse stream"));
         // no lists yet: empty lists, masks and grid until the first build (which the flag forces)
         if (cudaMemsetAsync(S.vl_rebuild, 0xFF, sizeof(uint32_t), s->stream) != cudaSuccess ||
+            cudaMemsetAsync(S.vl_gone, 0, sizeof(uint32_t), s->stream) != cudaSuccess ||
             cudaMemsetAsync(s->vl_builds, 0, sizeof(unsigned long long), s->stream) != cudaSuccess ||
             cudaMemsetAsync(G.vcount, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
             cudaMemsetAsync(G.vmask, 0, n * sizeof(unsigned long long), s->stream) != cudaSuccess ||
@@ -571,7 +573,10 @@ extern "C" int rrsph_upload(rrsph_solver* s, const double* r, uint32_t stride, c
     init.dt = s->params.dt;
     std::memcpy(s->h_scal, &init, sizeof(init));
     RRSPH_CUDA_TRY(cudaMemcpyAsync(s->scal, s->h_scal, sizeof(init), cudaMemcpyHostToDevice, st));
-    if (S.vl_rebuild) RRSPH_CUDA_TRY(cudaMemsetAsync(S.vl_rebuild, 0xFF, sizeof(uint32_t), st));
+    if (S.vl_rebuild) {  // the next key pass checks the uploaded positions against the last build
+        rrsph::launch_verlet_upload_check(S.vl_rebuild, S.vl_gone, st);
+        s->launches++;
+    }
     RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
     s->step_index = 0;
     s->keys_ready = false;

@@ -533,3 +533,44 @@ def test_neighbour_reuse_graph_and_direct_launches_agree(gpu_available):
     assert out[0][2] == out[1][2] + 25  # a graph step also launches the kernel that picks its branch
     for k in ("r", "v", "rho", "p"):
         assert np.array_equal(out[0][0][k], out[1][0][k]), k
+
+
+def test_neighbour_reuse_across_uploads(gpu_available):
+    """An upload keeps the candidate lists when every particle is within half
+    the skin of the last build and the build left no particle out; one that
+    re-admits a particle the build saw as non-existent forces a rebuild. The
+    results equal a fresh solver's either way."""
+    from sph2d_gb300 import Solver
+
+    case = _dam(nx=60, ny=30)
+    p = case.params()
+
+    def fresh(itype, steps):
+        with Solver(p, "mixed") as f:
+            f.upload(case.r, case.v, case.rho, itype)
+            f.step(steps, 0.0)
+            return f.download()
+
+    with Solver(p, "mixed") as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        s.step(5, 0.0)
+        b1 = s.neighbour_rebuilds()
+        s.upload(case.r, case.v, case.rho, case.itype)
+        s.step(5, 0.0)
+        assert s.neighbour_rebuilds() == b1  # same start: the lists still hold
+        again = s.download()
+        gone = case.itype.copy()
+        gone[0] = 0
+        s.upload(case.r, case.v, case.rho, gone)
+        s.set_neighbour_reuse(True)  # rebuild now, with particle 0 left out
+        s.step(1, 0.0)
+        b2 = s.neighbour_rebuilds()
+        assert b2 == b1 + 1
+        s.upload(case.r, case.v, case.rho, case.itype)  # particle 0 exists again
+        s.step(1, 0.0)
+        assert s.neighbour_rebuilds() == b2 + 1
+        back = s.download()
+    ref5, ref1 = fresh(case.itype, 5), fresh(case.itype, 1)
+    for k in ("r", "v", "rho", "p"):
+        assert np.array_equal(again[k], ref5[k]), k
+        assert np.array_equal(back[k], ref1[k]), k
