@@ -238,6 +238,12 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_mixed(DevParams P
 // update_acceleration's inner loop (UpdateAcceleration.cpp:66-97).
 template <int DIM, int SKF>
 struct ForceAcc {
+    // Lennard-Jones repulsion of a boundary neighbour (ExtForce.h), over |diff|.
+    static __device__ __forceinline__ float lj_coef(const MixedF& M, float inv_dist) {
+        const float rn = M.lj_rr0 * inv_dist;
+        const float rn2 = rn * rn, rn4 = rn2 * rn2, rn8 = rn4 * rn4;
+        return M.lj_D * (rn8 * rn4 - rn4) * (inv_dist * inv_dist);
+    }
     const DevParams& P;
     const Sorted& G;
     float4 vj;
@@ -258,11 +264,7 @@ struct ForceAcc {
         const float dist = d2 * inv_dist;
         const float q = dist * M.inv_h;
         float m = 0.0f;  // coefficient of diff (= r_i - r_j) in this pair's acceleration
-        if (ext && ti < 0 && dist < M.lj_rr0) {
-            const float rn = M.lj_rr0 * inv_dist;
-            const float rn2 = rn * rn, rn4 = rn2 * rn2, rn8 = rn4 * rn4;
-            m -= M.lj_D * (rn8 * rn4 - rn4) * (inv_dist * inv_dist);
-        }
+        if (ext && ti < 0 && dist < M.lj_rr0) m -= lj_coef(M, inv_dist);
         const float rhoi = vi.w;
         const float sc = kernel_dwdr_scalef(intf_skf, M.kf[intf_skf], q, inv_dist, M.inv_h);
         if (intf) {
@@ -299,6 +301,27 @@ struct ForceAcc {
             cvy += (vi.y - vj.y) * mv;
             if (DIM == 3) cvz += (vi.z - vj.z) * mv;
         }
+    }
+    // pair_with for the common method set, 2D: pressure form 2, Monaghan
+    // viscosity, cubic kernel, no artificial pressure or XSPH; vi.z holds the
+    // neighbour's p/rho^2. The same arithmetic as pair_with with those switches.
+    __device__ __forceinline__ void pair_std(const float4 vi, float dx, float dy, float d2, int32_t ti) {
+        const MixedF& M = P.mf;
+        const float inv_dist = rsqrtf(d2);
+        const float dist = d2 * inv_dist;
+        const float q = dist * M.inv_h;
+        float m = 0.0f;
+        if (ext && ti < 0 && dist < M.lj_rr0) m -= lj_coef(M, inv_dist);
+        const float rhoi = vi.w;
+        const float sc = kernel_dwdr_scalef(1, M.kf[1], q, inv_dist, M.inv_h);
+        m += sc * (vi.z + prj.y) * M.mass;
+        const float vr = -((vj.x - vi.x) * dx + (vj.y - vi.y) * dy);
+        const float mu = fminf(__fdividef(M.h * vr, d2 + M.etq_h2), 0.0f);
+        arvmu = fmaxf(arvmu, -mu);
+        const float piv = __fdividef((M.av_beta * mu - M.av_alpha_c) * mu, 0.5f * (rhoi + rhoj));
+        m += sc * piv * M.mass;
+        cax += dx * m;
+        cay += dy * m;
     }
 };
 
@@ -597,6 +620,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
 #pragma unroll
                     for (int j = 0; j < kVlBatch; j++)
                         pb[j] = en[j] != kVlNone ? G.P4[en[j] & 0x07FFFFFFu] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    uint32_t gm = 0;  // this group's neighbours, bit j for entry e0 + j
 #pragma unroll
                     for (int j = 0; j < kVlBatch; j++) {
                         if (en[j] == kVlNone) break;
@@ -612,10 +636,11 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
                         const float dx = pb[j].x + shx, dy = pb[j].y + shy;
                         const float d2 = dx * dx + dy * dy;
                         if (!within_cutoff<2>(P, S, G, en[j] & 0x07FFFFFFu, k, d2)) continue;
-                        cnt++;
-                        mask |= 1ull << (e0 + j);
+                        gm |= 1u << j;
                         part += kernel_wf(skf, f, d2 * rsqrtf(d2) * M.inv_h);
                     }
+                    cnt += __popc(gm);
+                    mask |= (unsigned long long)gm << e0;
                 }
                 if (cur >= 0) acc.add(M.mass * part);
             } else {
@@ -650,8 +675,10 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
         const float d = ((acc.s - M.rho0_minus_w0_hi) - acc.c) - M.rho0_minus_w0_lo;
         const float rho = M.rho0 + d;
         const float pr = eos_pf(M, d);
-        G.V4[k].w = rho;
-        G.PR[k] = make_float2(pr, pr * __frcp_rn(rho * rho));
+        const float2 prr = make_float2(pr, pr * __frcp_rn(rho * rho));
+        // V4.zw = (the pressure the force pass reads of a neighbour: p with form 1, else p/rho^2, rho)
+        reinterpret_cast<float2*>(G.V4 + k)[1] = make_float2(P.intf_form == 1 ? prr.x : prr.y, rho);
+        G.PR[k] = prr;
         S.rho[id] = P.rho0 + f2d(d);
         S.p[id] = f2d(pr);
     }
@@ -659,9 +686,13 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
 }
 
 // update_acceleration over this step's neighbours: the list entries the
-// density pass marked (or the stencil search for an overflowed list).
-template <int SKF>
-__global__ void __launch_bounds__(kMaxGatherThreads) k_forces_verlet(DevParams P, State S, Sorted G,
+// density pass marked (or the stencil search for an overflowed list). A
+// neighbour's pressure comes with its velocity and density (V4.z). STD: the
+// common method set of ForceAcc::pair_std, fixed at compile time. At most 64
+// registers (4 blocks of 256 threads per SM): the gather hides its L1/L2
+// latency with warps.
+template <int SKF, bool STD>
+__global__ void __launch_bounds__(kMaxGatherThreads, 4) k_forces_verlet(DevParams P, State S, Sorted G,
                                                                     StepScalars* __restrict__ scal,
                                                                     uint32_t* __restrict__ flags) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -696,7 +727,6 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_forces_verlet(DevParams P
                     // then their data, loaded together so that the loads overlap
                     uint32_t en[kVlForceBatch];
                     float4 pb[kVlForceBatch], vb[kVlForceBatch];
-                    float2 rb[kVlForceBatch];
 #pragma unroll
                     for (int j = 0; j < kVlForceBatch; j++) {
                         if (left) {
@@ -712,7 +742,6 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_forces_verlet(DevParams P
                         const uint32_t i = en[j] & 0x07FFFFFFu;
                         pb[j] = G.P4[i];
                         vb[j] = G.V4[i];
-                        rb[j] = G.PR[i];
                     }
 #pragma unroll
                     for (int j = 0; j < kVlForceBatch; j++) {
@@ -733,7 +762,14 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_forces_verlet(DevParams P
                             shy = (float)(c % 5 - 2) * M.cell - pj4.y;
                         }
                         const float dx = pb[j].x + shx, dy = pb[j].y + shy;
-                        F.pair_with(vb[j], rb[j], dx, dy, 0.0f, dx * dx + dy * dy, __float_as_int(pb[j].w));
+                        if (STD) {
+                            F.pair_std(vb[j], dx, dy, dx * dx + dy * dy, __float_as_int(pb[j].w));
+                        } else {
+                            const float z = vb[j].z;  // p (form 1) or p/rho^2, as the density pass wrote it
+                            const float2 pri = F.form1 ? make_float2(z, z * __frcp_rn(vb[j].w * vb[j].w))
+                                                       : make_float2(z, z);
+                            F.pair_with(vb[j], pri, dx, dy, 0.0f, dx * dx + dy * dy, __float_as_int(pb[j].w));
+                        }
                     }
                 }
                 if (cur >= 0) {
@@ -820,8 +856,10 @@ void launch_density_verlet(const DevParams& P, const State& S, const Sorted& G, 
 void launch_forces_verlet(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
                           cudaStream_t st, int threads) {
     const unsigned blocks = (P.n + threads - 1) / threads;
-    if (P.all_cubic) k_forces_verlet<1><<<blocks, threads, 0, st>>>(P, S, G, scal, flags);
-    else k_forces_verlet<0><<<blocks, threads, 0, st>>>(P, S, G, scal, flags);
+    const bool std_terms = P.all_cubic && P.intf_form != 1 && P.art_visc && !P.art_pressure && !P.avg_vel;
+    if (std_terms) k_forces_verlet<1, true><<<blocks, threads, 0, st>>>(P, S, G, scal, flags);
+    else if (P.all_cubic) k_forces_verlet<1, false><<<blocks, threads, 0, st>>>(P, S, G, scal, flags);
+    else k_forces_verlet<0, false><<<blocks, threads, 0, st>>>(P, S, G, scal, flags);
 }
 
 template <int DIM>
