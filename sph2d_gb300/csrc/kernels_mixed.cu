@@ -586,6 +586,22 @@ __global__ void k_vl_reorder(DevParams P, State S, Sorted G) {
     G.V4[k] = make_float4(v.x, v.y, 0.0f, 0.0f);  // .w: the density pass writes it
 }
 
+// Stencil offset of a list entry's 5-bit cell code (dx + 2) * 5 + (dy + 2):
+// cx = dx + 2, cy = dy + 2 (c / 5 as (c * 13) >> 6, exact for c < 32).
+__device__ __forceinline__ void vl_code_xy(uint32_t en, uint32_t& cx, uint32_t& cy) {
+    const uint32_t c = en >> 27;
+    cx = (c * 13u) >> 6;
+    cy = c - 5u * cx;
+}
+
+// The cubic W(q) of kernel_wf as selects: every lane runs the same instructions.
+__device__ __forceinline__ float cubic_wf_sel(float f, float q) {
+    const float t = 2.0f - q;
+    const float w1 = f * ((2.0f / 3.0f - q * q) + q * q * q * 0.5f);
+    const float w2 = f * ((1.0f / 6.0f) * (t * t * t));
+    return q <= 1.0f ? w1 : (q <= 2.0f ? w2 : 0.0f);
+}
+
 // density_sum (Density.h:25-61) + EOS over the candidate list: the entries
 // within the cutoff are this step's neighbours (recorded in vmask for the
 // force pass). A particle whose list overflowed searches the stencil cells
@@ -610,9 +626,11 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
             const uint32_t vc = G.vcount[k];
             if (vc != kListOver) {
                 const uint4* row = reinterpret_cast<const uint4*>(G.vlist + (size_t)k * kVerletCap);
-                int cur = -1;
-                float shx = 0.0f, shy = 0.0f, part = 0.0f;
-                // groups of four entries (one load), then their particles, loaded together
+                // shift of stencil offset (cx, cy) = (cx - 2, cy - 2) cells, relative to this particle
+                const float bx = -2.0f * M.cell - pj.x, by = -2.0f * M.cell - pj.y;
+                // groups of four entries (one load), then their particles, loaded together;
+                // the body has no branch but the rare guard-band test, and every term
+                // is added with compensation
                 for (uint32_t e0 = 0; e0 < vc; e0 += kVlBatch) {
                     const uint4 w = row[e0 >> 2];
                     const uint32_t en[kVlBatch] = {w.x, w.y, w.z, w.w};
@@ -623,26 +641,22 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
                     uint32_t gm = 0;  // this group's neighbours, bit j for entry e0 + j
 #pragma unroll
                     for (int j = 0; j < kVlBatch; j++) {
-                        if (en[j] == kVlNone) break;
-                        const int c = (int)(en[j] >> 27);
-                        if (c != cur) {
-                            if (cur >= 0) acc.add(M.mass * part);
-                            part = 0.0f;
-                            cur = c;
-                            shx = (float)(c / 5 - 2) * M.cell - pj.x;
-                            shy = (float)(c % 5 - 2) * M.cell - pj.y;
-                        }
-                        if (__float_as_int(pb[j].w) == P.type_non_existent) continue;
-                        const float dx = pb[j].x + shx, dy = pb[j].y + shy;
+                        uint32_t cx, cy;
+                        vl_code_xy(en[j], cx, cy);
+                        const float dx = pb[j].x + fmaf((float)cx, M.cell, bx);
+                        const float dy = pb[j].y + fmaf((float)cy, M.cell, by);
                         const float d2 = dx * dx + dy * dy;
-                        if (!within_cutoff<2>(P, S, G, en[j] & 0x07FFFFFFu, k, d2)) continue;
-                        gm |= 1u << j;
-                        part += kernel_wf(skf, f, d2 * rsqrtf(d2) * M.inv_h);
+                        bool in = en[j] != kVlNone && __float_as_int(pb[j].w) != P.type_non_existent &&
+                                  d2 < M.cut2_hi;
+                        if (in && !(d2 < M.cut2_lo)) in = within_cutoff<2>(P, S, G, en[j] & 0x07FFFFFFu, k, d2);
+                        const float q = d2 * rsqrtf(d2) * M.inv_h;
+                        const float wv = SKF == 1 ? cubic_wf_sel(f, q) : kernel_wf(skf, f, q);
+                        acc.add(in ? M.mass * wv : 0.0f);
+                        gm |= (uint32_t)in << j;
                     }
                     cnt += __popc(gm);
                     mask |= (unsigned long long)gm << e0;
                 }
-                if (cur >= 0) acc.add(M.mass * part);
             } else {
                 const Stencil<2> st(P, G.key[k]);
 #pragma unroll 1
@@ -720,8 +734,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads, 4) k_forces_verlet(DevParam
             if (vc != kListOver) {
                 const uint32_t* row = G.vlist + (size_t)k * kVerletCap;
                 unsigned long long left = G.vmask[k];
-                int cur = -1;
-                float shx = 0.0f, shy = 0.0f;
+                const float bx = -2.0f * M.cell - pj4.x, by = -2.0f * M.cell - pj4.y;
                 while (left) {
                     // the next neighbours' list words (this particle's row, cached),
                     // then their data, loaded together so that the loads overlap
@@ -743,25 +756,16 @@ __global__ void __launch_bounds__(kMaxGatherThreads, 4) k_forces_verlet(DevParam
                         pb[j] = G.P4[i];
                         vb[j] = G.V4[i];
                     }
+                    // each pair's terms are added with compensation (no per-cell
+                    // partial sums, whose flushes would split the warp)
 #pragma unroll
                     for (int j = 0; j < kVlForceBatch; j++) {
                         if (en[j] == kVlNone) continue;
-                        const int c = (int)(en[j] >> 27);
-                        if (c != cur) {
-                            if (cur >= 0) {
-                                ax.add(F.cax);
-                                ay.add(F.cay);
-                                if (F.avel) {
-                                    avx.add(F.cvx);
-                                    avy.add(F.cvy);
-                                }
-                            }
-                            F.cax = F.cay = F.cvx = F.cvy = 0.0f;
-                            cur = c;
-                            shx = (float)(c / 5 - 2) * M.cell - pj4.x;
-                            shy = (float)(c % 5 - 2) * M.cell - pj4.y;
-                        }
-                        const float dx = pb[j].x + shx, dy = pb[j].y + shy;
+                        uint32_t cx, cy;
+                        vl_code_xy(en[j], cx, cy);
+                        const float dx = pb[j].x + fmaf((float)cx, M.cell, bx);
+                        const float dy = pb[j].y + fmaf((float)cy, M.cell, by);
+                        F.cax = F.cay = F.cvx = F.cvy = 0.0f;
                         if (STD) {
                             F.pair_std(vb[j], dx, dy, dx * dx + dy * dy, __float_as_int(pb[j].w));
                         } else {
@@ -770,14 +774,12 @@ __global__ void __launch_bounds__(kMaxGatherThreads, 4) k_forces_verlet(DevParam
                                                        : make_float2(z, z);
                             F.pair_with(vb[j], pri, dx, dy, 0.0f, dx * dx + dy * dy, __float_as_int(pb[j].w));
                         }
-                    }
-                }
-                if (cur >= 0) {
-                    ax.add(F.cax);
-                    ay.add(F.cay);
-                    if (F.avel) {
-                        avx.add(F.cvx);
-                        avy.add(F.cvy);
+                        ax.add(F.cax);
+                        ay.add(F.cay);
+                        if (!STD && F.avel) {
+                            avx.add(F.cvx);
+                            avy.add(F.cvy);
+                        }
                     }
                 }
             } else {
