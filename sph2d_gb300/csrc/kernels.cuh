@@ -59,12 +59,13 @@ struct Sorted {
     // stencil cell c is a neighbour; word 9 = stencil cells with more than 32
     // particles (searched again by the force pass). Null where unused.
     uint32_t* nbmask;
-    // 2D mixed step with neighbour reuse: per particle a row of kVerletCap
-    // candidates (list[k * kVerletCap + e] = sorted index | cell code << 27,
-    // code = (dx + 2) * 5 + (dy + 2) for the candidate's cell offset; the last
-    // group of four is padded with kVlNone), vcount[k] = candidates (kListOver:
-    // too many, searched instead), vmask[k] = the candidates within the cutoff
-    // in this step.
+    // 2D mixed step with neighbour reuse: up to kVerletCap candidates per
+    // particle, sorted index | cell code << 27 with code = (dx + 2) * 5 + (dy + 2)
+    // for the candidate's cell offset, stored in slabs of four: entries 4g..4g+3
+    // of particle k are the uint4 at (uint4*)list + g * n + k (the lanes of a
+    // warp read neighbouring uint4s), the last group padded with kVlNone;
+    // vcount[k] = candidates (kListOver: too many, searched instead), vmask[k] =
+    // the candidates within the cutoff in this step.
     uint32_t* vlist;
     uint32_t* vcount;
     unsigned long long* vmask;

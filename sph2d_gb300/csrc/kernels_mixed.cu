@@ -504,14 +504,12 @@ __global__ void k_vl_upload_check(uint32_t* __restrict__ rebuild, const uint32_t
     if (*rebuild != 0xFFFFFFFFu) *rebuild = *gone ? 1u : 0u;
 }
 
-// After this step's grid (sort + reorder): each particle's candidates, through
-// a per-thread list in shared memory ([kVerletCap][blockDim], conflict-free)
-// copied to the particle's row of the global list four entries per store. The
-// cell equals the cutoff, so a candidate within cutoff + skin can lie two
-// cells away: a particle within one skin of a cell edge also searches the
-// cells beyond that edge.
+// After this step's grid (sort + reorder): each particle's candidates, four
+// entries gathered in registers and stored as one uint4 into the group's slab
+// (the lanes of a warp store neighbouring uint4s). The cell equals the cutoff,
+// so a candidate within cutoff + skin can lie two cells away: a particle within
+// one skin of a cell edge also searches the cells beyond that edge.
 __global__ void __launch_bounds__(kMaxGatherThreads) k_vl_build(DevParams P, State S, Sorted G) {
-    extern __shared__ uint32_t s_list[];
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= P.n) return;
     const MixedF& M = P.mf;
@@ -520,7 +518,8 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_vl_build(DevParams P, Sta
     const uint32_t cx = second_bits(key), cy = second_bits(key >> 1);
     S.bcxy[id] = cx | (cy << 16);
     S.boff[id] = make_float2(pj.x, pj.y);
-    const uint32_t bd = blockDim.x, t = threadIdx.x;
+    uint4* const slab = reinterpret_cast<uint4*>(G.vlist) + k;  // group g at slab[g * n]
+    uint4 buf = make_uint4(kVlNone, kVlNone, kVlNone, kVlNone);
     uint32_t nl = 0;
     if (__float_as_int(pj.w) == P.type_non_existent) atomicOr(S.vl_gone, 1u);
     if (__float_as_int(pj.w) != P.type_non_existent) {
@@ -547,23 +546,24 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_vl_build(DevParams P, Sta
                     if (__float_as_int(pi.w) == P.type_non_existent) continue;  // stays non-existent
                     const float ddx = pi.x + shx, ddy = pi.y + shy;
                     if (ddx * ddx + ddy * ddy < P.vl_cut2) {
-                        if (nl < (uint32_t)kVerletCap) s_list[nl * bd + t] = i | code;
+                        if (nl < (uint32_t)kVerletCap) {
+                            const uint32_t v = i | code, slot = nl & 3u;
+                            buf.x = slot == 0 ? v : buf.x;
+                            buf.y = slot == 1 ? v : buf.y;
+                            buf.z = slot == 2 ? v : buf.z;
+                            buf.w = slot == 3 ? v : buf.w;
+                            if (slot == 3) {
+                                slab[(size_t)(nl >> 2) * P.n] = buf;
+                                buf = make_uint4(kVlNone, kVlNone, kVlNone, kVlNone);
+                            }
+                        }
                         nl++;
                     }
                 }
             }
         }
     }
-    const uint32_t m = nl < (uint32_t)kVerletCap ? nl : (uint32_t)kVerletCap;
-    uint4* row = reinterpret_cast<uint4*>(G.vlist + (size_t)k * kVerletCap);  // 256-byte aligned rows
-    for (uint32_t e = 0; e < m; e += 4) {
-        uint4 w;
-        w.x = s_list[e * bd + t];
-        w.y = e + 1 < m ? s_list[(e + 1) * bd + t] : kVlNone;
-        w.z = e + 2 < m ? s_list[(e + 2) * bd + t] : kVlNone;
-        w.w = e + 3 < m ? s_list[(e + 3) * bd + t] : kVlNone;
-        row[e >> 2] = w;
-    }
+    if (nl < (uint32_t)kVerletCap && (nl & 3u)) slab[(size_t)(nl >> 2) * P.n] = buf;  // the padded last group
     G.vcount[k] = nl <= (uint32_t)kVerletCap ? nl : kListOver;
     if (nl > (uint32_t)kVerletCap) {  // its search needs a fresh grid each step
         atomicOr(S.vl_rebuild, 1u);
@@ -625,14 +625,14 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
         if (tj != P.type_non_existent) {
             const uint32_t vc = G.vcount[k];
             if (vc != kListOver) {
-                const uint4* row = reinterpret_cast<const uint4*>(G.vlist + (size_t)k * kVerletCap);
+                const uint4* slab = reinterpret_cast<const uint4*>(G.vlist) + k;  // group g at slab[g * n]
                 // shift of stencil offset (cx, cy) = (cx - 2, cy - 2) cells, relative to this particle
                 const float bx = -2.0f * M.cell - pj.x, by = -2.0f * M.cell - pj.y;
                 // groups of four entries (one load), then their particles, loaded together;
                 // the body has no branch but the rare guard-band test, and every term
                 // is added with compensation
                 for (uint32_t e0 = 0; e0 < vc; e0 += kVlBatch) {
-                    const uint4 w = row[e0 >> 2];
+                    const uint4 w = slab[(size_t)(e0 >> 2) * P.n];
                     const uint32_t en[kVlBatch] = {w.x, w.y, w.z, w.w};
                     float4 pb[kVlBatch];
 #pragma unroll
@@ -732,7 +732,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads, 4) k_forces_verlet(DevParam
         if (tj != P.type_non_existent) {
             const uint32_t vc = G.vcount[k];
             if (vc != kListOver) {
-                const uint32_t* row = G.vlist + (size_t)k * kVerletCap;
+                const uint32_t* slab = G.vlist + (size_t)k * 4;  // entry e at slab[(e / 4) * 4n + e % 4]
                 unsigned long long left = G.vmask[k];
                 const float bx = -2.0f * M.cell - pj4.x, by = -2.0f * M.cell - pj4.y;
                 while (left) {
@@ -743,7 +743,8 @@ __global__ void __launch_bounds__(kMaxGatherThreads, 4) k_forces_verlet(DevParam
 #pragma unroll
                     for (int j = 0; j < kVlForceBatch; j++) {
                         if (left) {
-                            en[j] = row[__ffsll((long long)left) - 1];
+                            const uint32_t e = (uint32_t)__ffsll((long long)left) - 1u;
+                            en[j] = slab[(size_t)(e >> 2) * 4 * P.n + (e & 3u)];
                             left &= left - 1;
                         } else {
                             en[j] = kVlNone;
@@ -842,9 +843,8 @@ void launch_verlet_upload_check(uint32_t* rebuild, const uint32_t* gone, cudaStr
     k_vl_upload_check<<<1, 1, 0, st>>>(rebuild, gone);
 }
 void launch_verlet_build(const DevParams& P, const State& S, const Sorted& G, cudaStream_t st) {
-    constexpr int kBuildThreads = 128;  // the per-thread lists take 32 KB of shared memory
-    const size_t smem = (size_t)kVerletCap * kBuildThreads * sizeof(uint32_t);
-    k_vl_build<<<(P.n + kBuildThreads - 1) / kBuildThreads, kBuildThreads, smem, st>>>(P, S, G);
+    constexpr int kBuildThreads = 128;
+    k_vl_build<<<(P.n + kBuildThreads - 1) / kBuildThreads, kBuildThreads, 0, st>>>(P, S, G);
 }
 void launch_verlet_reorder(const DevParams& P, const State& S, const Sorted& G, cudaStream_t st) {
     k_vl_reorder<<<(P.n + 255) / 256, 256, 0, st>>>(P, S, G);
