@@ -42,11 +42,12 @@ L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
 
 # Algorithmic bytes of the dominant kernel (the force gather, k_forces_verlet)
 # of the FP32-mixed 2D step with neighbour reuse: per particle it reads its id 4,
-# position+type float4 16, velocity+density float4 16, (p, p/rho^2) float2 8,
-# list count 4 and this step's neighbour mask 8, and writes a.x, a.y as double
-# 16; per neighbour pair it reads one 4-byte list word. The neighbours' own data
-# are re-reads of particles other threads load (L1/L2), not algorithmic bytes.
-FORCES_REUSE_BYTES_PER_PARTICLE = 4 + 16 + 16 + 8 + 4 + 8 + 16
+# position+type float4 16, velocity+pressure+density float4 16, (p, p/rho^2)
+# float2 8, candidate count 4 and neighbour count 4, and writes a.x, a.y as
+# double 16; per neighbour pair it reads one 4-byte word of this step's
+# neighbour list. The neighbours' own data are re-reads of particles other
+# threads load (L1/L2), not algorithmic bytes.
+FORCES_REUSE_BYTES_PER_PARTICLE = 4 + 16 + 16 + 8 + 4 + 4 + 16
 FORCES_REUSE_BYTES_PER_PAIR = 4
 FORCES_FP64_BYTES_PER_PARTICLE_2D = 4 + 4 + 16 + 4 + 16 + 8 + 8 + 16
 

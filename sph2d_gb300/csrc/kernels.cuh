@@ -64,11 +64,13 @@ struct Sorted {
     // for the candidate's cell offset, stored in slabs of four: entries 4g..4g+3
     // of particle k are the uint4 at (uint4*)list + g * n + k (the lanes of a
     // warp read neighbouring uint4s), the last group padded with kVlNone;
-    // vcount[k] = candidates (kListOver: too many, searched instead), vmask[k] =
-    // the candidates within the cutoff in this step.
+    // vcount[k] = candidates (kListOver: too many, searched instead). This
+    // step's neighbours (the candidates within the cutoff, in list order) in the
+    // same slab layout: nlist, ncount[k] of them; words past ncount are stale.
     uint32_t* vlist;
     uint32_t* vcount;
-    unsigned long long* vmask;
+    uint32_t* nlist;
+    uint32_t* ncount;
 };
 
 // Sources the reorder gathers for the force velocity / density.

@@ -603,8 +603,8 @@ __device__ __forceinline__ float cubic_wf_sel(float f, float q) {
 }
 
 // density_sum (Density.h:25-61) + EOS over the candidate list: the entries
-// within the cutoff are this step's neighbours (recorded in vmask for the
-// force pass). A particle whose list overflowed searches the stencil cells
+// within the cutoff are this step's neighbours (written to nlist for the force
+// pass). A particle whose list overflowed searches the stencil cells
 // (the grid is rebuilt every step while one does).
 template <int SKF>
 __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams P, State S, Sorted G,
@@ -621,7 +621,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
         const int skf = SKF ? SKF : P.density_skf;
         const float f = M.kf[skf];
         Kahan acc{0.0f, 0.0f};
-        unsigned long long mask = 0ull;
+        uint32_t* const nslab = G.nlist + (size_t)k * 4;  // neighbour e at nslab[(e / 4) * 4n + e % 4]
         if (tj != P.type_non_existent) {
             const uint32_t vc = G.vcount[k];
             if (vc != kListOver) {
@@ -638,7 +638,6 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
 #pragma unroll
                     for (int j = 0; j < kVlBatch; j++)
                         pb[j] = en[j] != kVlNone ? G.P4[en[j] & 0x07FFFFFFu] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                    uint32_t gm = 0;  // this group's neighbours, bit j for entry e0 + j
 #pragma unroll
                     for (int j = 0; j < kVlBatch; j++) {
                         uint32_t cx, cy;
@@ -652,10 +651,9 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
                         const float q = d2 * rsqrtf(d2) * M.inv_h;
                         const float wv = SKF == 1 ? cubic_wf_sel(f, q) : kernel_wf(skf, f, q);
                         acc.add(in ? M.mass * wv : 0.0f);
-                        gm |= (uint32_t)in << j;
+                        if (in) nslab[(size_t)(cnt >> 2) * 4 * P.n + (cnt & 3u)] = en[j];
+                        cnt += in;
                     }
-                    cnt += __popc(gm);
-                    mask |= (unsigned long long)gm << e0;
                 }
             } else {
                 const Stencil<2> st(P, G.key[k]);
@@ -684,7 +682,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
                 }
             }
         }
-        G.vmask[k] = mask;
+        G.ncount[k] = G.vcount[k] != kListOver ? cnt : 0u;
         if (cnt > P.max_nb - 1) atomicOr(flags, RRSPH_FLAG_NEIGHBOUR_OVERFLOW);
         const float d = ((acc.s - M.rho0_minus_w0_hi) - acc.c) - M.rho0_minus_w0_lo;
         const float rho = M.rho0 + d;
@@ -732,54 +730,51 @@ __global__ void __launch_bounds__(kMaxGatherThreads, 4) k_forces_verlet(DevParam
         if (tj != P.type_non_existent) {
             const uint32_t vc = G.vcount[k];
             if (vc != kListOver) {
-                const uint32_t* slab = G.vlist + (size_t)k * 4;  // entry e at slab[(e / 4) * 4n + e % 4]
-                unsigned long long left = G.vmask[k];
+                // this step's neighbours, four list words per load (the lanes of a
+                // warp load neighbouring uint4s), their data two at a time
+                const uint32_t nc = G.ncount[k];
+                const uint4* nslab = reinterpret_cast<const uint4*>(G.nlist) + k;  // group g at nslab[g * n]
                 const float bx = -2.0f * M.cell - pj4.x, by = -2.0f * M.cell - pj4.y;
-                while (left) {
-                    // the next neighbours' list words (this particle's row, cached),
-                    // then their data, loaded together so that the loads overlap
-                    uint32_t en[kVlForceBatch];
-                    float4 pb[kVlForceBatch], vb[kVlForceBatch];
+                for (uint32_t e0 = 0; e0 < nc; e0 += 4) {
+                    const uint4 w = nslab[(size_t)(e0 >> 2) * P.n];
+                    const uint32_t eg[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
-                    for (int j = 0; j < kVlForceBatch; j++) {
-                        if (left) {
-                            const uint32_t e = (uint32_t)__ffsll((long long)left) - 1u;
-                            en[j] = slab[(size_t)(e >> 2) * 4 * P.n + (e & 3u)];
-                            left &= left - 1;
-                        } else {
-                            en[j] = kVlNone;
+                    for (int h = 0; h < 4; h += kVlForceBatch) {
+                        uint32_t en[kVlForceBatch];
+                        float4 pb[kVlForceBatch], vb[kVlForceBatch];
+#pragma unroll
+                        for (int j = 0; j < kVlForceBatch; j++) en[j] = e0 + h + j < nc ? eg[h + j] : kVlNone;
+#pragma unroll
+                        for (int j = 0; j < kVlForceBatch; j++) {
+                            if (en[j] == kVlNone) continue;
+                            const uint32_t i = en[j] & 0x07FFFFFFu;
+                            pb[j] = G.P4[i];
+                            vb[j] = G.V4[i];
                         }
-                    }
+                        // each pair's terms are added with compensation (no per-cell
+                        // partial sums, whose flushes would split the warp)
 #pragma unroll
-                    for (int j = 0; j < kVlForceBatch; j++) {
-                        if (en[j] == kVlNone) continue;
-                        const uint32_t i = en[j] & 0x07FFFFFFu;
-                        pb[j] = G.P4[i];
-                        vb[j] = G.V4[i];
-                    }
-                    // each pair's terms are added with compensation (no per-cell
-                    // partial sums, whose flushes would split the warp)
-#pragma unroll
-                    for (int j = 0; j < kVlForceBatch; j++) {
-                        if (en[j] == kVlNone) continue;
-                        uint32_t cx, cy;
-                        vl_code_xy(en[j], cx, cy);
-                        const float dx = pb[j].x + fmaf((float)cx, M.cell, bx);
-                        const float dy = pb[j].y + fmaf((float)cy, M.cell, by);
-                        F.cax = F.cay = F.cvx = F.cvy = 0.0f;
-                        if (STD) {
-                            F.pair_std(vb[j], dx, dy, dx * dx + dy * dy, __float_as_int(pb[j].w));
-                        } else {
-                            const float z = vb[j].z;  // p (form 1) or p/rho^2, as the density pass wrote it
-                            const float2 pri = F.form1 ? make_float2(z, z * __frcp_rn(vb[j].w * vb[j].w))
-                                                       : make_float2(z, z);
-                            F.pair_with(vb[j], pri, dx, dy, 0.0f, dx * dx + dy * dy, __float_as_int(pb[j].w));
-                        }
-                        ax.add(F.cax);
-                        ay.add(F.cay);
-                        if (!STD && F.avel) {
-                            avx.add(F.cvx);
-                            avy.add(F.cvy);
+                        for (int j = 0; j < kVlForceBatch; j++) {
+                            if (en[j] == kVlNone) continue;
+                            uint32_t cx, cy;
+                            vl_code_xy(en[j], cx, cy);
+                            const float dx = pb[j].x + fmaf((float)cx, M.cell, bx);
+                            const float dy = pb[j].y + fmaf((float)cy, M.cell, by);
+                            F.cax = F.cay = F.cvx = F.cvy = 0.0f;
+                            if (STD) {
+                                F.pair_std(vb[j], dx, dy, dx * dx + dy * dy, __float_as_int(pb[j].w));
+                            } else {
+                                const float z = vb[j].z;  // p (form 1) or p/rho^2, as the density pass wrote it
+                                const float2 pri = F.form1 ? make_float2(z, z * __frcp_rn(vb[j].w * vb[j].w))
+                                                           : make_float2(z, z);
+                                F.pair_with(vb[j], pri, dx, dy, 0.0f, dx * dx + dy * dy, __float_as_int(pb[j].w));
+                            }
+                            ax.add(F.cax);
+                            ay.add(F.cay);
+                            if (!STD && F.avel) {
+                                avx.add(F.cvx);
+                                avy.add(F.cvy);
+                            }
                         }
                     }
                 }

@@ -467,7 +467,7 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
         if (!d3 && !cont) {  // neighbour reuse
             A(S.cxy, n); A(S.bcxy, n); A(S.boff, n); A(S.vl_rebuild, 2); A(s->vl_builds, 1);
             S.vl_gone = S.vl_rebuild + 1;
-            A(G.vlist, (size_t)rrsph::kVerletCap * n); A(G.vcount, n); A(G.vmask, n);
+            A(G.vlist, (size_t)rrsph::kVerletCap * n); A(G.vcount, n); A(G.nlist, (size_t)rrsph::kVerletCap * n); A(G.ncount, n);
             A(G.keys_b, n); A(G.ids_b, n);
         }
         A(G.P4, n); A(G.V4, n); A(G.PR, n);
@@ -486,7 +486,7 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
             cudaMemsetAsync(S.vl_gone, 0, sizeof(uint32_t), s->stream) != cudaSuccess ||
             cudaMemsetAsync(s->vl_builds, 0, sizeof(unsigned long long), s->stream) != cudaSuccess ||
             cudaMemsetAsync(G.vcount, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
-            cudaMemsetAsync(G.vmask, 0, n * sizeof(unsigned long long), s->stream) != cudaSuccess ||
+            cudaMemsetAsync(G.ncount, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
             cudaMemsetAsync(S.bcxy, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
             cudaMemsetAsync(S.boff, 0, n * sizeof(float2), s->stream) != cudaSuccess ||
             cudaMemsetAsync(G.keys_a, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
