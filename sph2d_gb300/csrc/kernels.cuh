@@ -29,6 +29,7 @@ struct State {
     // 2D mixed step with neighbour reuse (null otherwise), id order:
     uint32_t* cxy;             // cell coordinates of the current position, x | y << 16
     uint32_t* bcxy;            // cell coordinates at the last list build
+    uint32_t* slot;            // cell-order index at the last list build
     float2* boff;              // offset from that cell's edge at the last list build
     uint32_t* vl_rebuild;      // non-zero: the next step rebuilds the grid and the lists
     uint32_t* vl_gone;         // the last build: bit 0 left out non-existent particles, bit 1 overflowed a list
@@ -114,7 +115,6 @@ void launch_verlet_reset(uint32_t* rebuild, uint32_t* gone, unsigned long long* 
 // non-existent particle (which may exist now); moves are checked by the key pass.
 void launch_verlet_upload_check(uint32_t* rebuild, const uint32_t* gone, cudaStream_t st);
 void launch_verlet_build(const DevParams& P, const State& S, const Sorted& G, cudaStream_t st);
-void launch_verlet_reorder(const DevParams& P, const State& S, const Sorted& G, cudaStream_t st);
 void launch_density_verlet(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
                            cudaStream_t st, int threads);
 void launch_forces_verlet(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,

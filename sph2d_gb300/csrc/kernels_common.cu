@@ -73,8 +73,16 @@ __device__ __forceinline__ void key_pass(const DevParams& P, const State& S, con
             S.cxy[i] = cx | (cy << 16);
             const uint32_t b = S.bcxy[i];
             const float2 bo = S.boff[i];
-            const float dx = ox + (float)((int)cx - (int)(b & 0xFFFFu)) * P.mf.cell - bo.x;
-            const float dy = oy + (float)((int)cy - (int)(b >> 16)) * P.mf.cell - bo.y;
+            // offset from the edge of the cell the particle had at the build
+            const float px = ox + (float)((int)cx - (int)(b & 0xFFFFu)) * P.mf.cell;
+            const float py = oy + (float)((int)cy - (int)(b >> 16)) * P.mf.cell;
+            // the next step's cell-order copies, at the particle's slot of the build
+            // (a step that rebuilds overwrites them in its new order)
+            const uint32_t k = S.slot[i];
+            G.P4[k] = make_float4(px, py, 0.0f, __int_as_float(S.itype[i]));
+            const float2 v = S.vpf2[i];
+            G.V4[k] = make_float4(v.x, v.y, 0.0f, 0.0f);  // .zw: the density pass writes them
+            const float dx = px - bo.x, dy = py - bo.y;
             const bool moved = !(dx * dx + dy * dy <= P.vl_half_skin2);
             const unsigned am = __activemask();
             const unsigned who = __ballot_sync(am, moved);

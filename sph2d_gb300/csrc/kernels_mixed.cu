@@ -517,6 +517,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_vl_build(DevParams P, Sta
     const float4 pj = G.P4[k];
     const uint32_t cx = second_bits(key), cy = second_bits(key >> 1);
     S.bcxy[id] = cx | (cy << 16);
+    S.slot[id] = k;
     S.boff[id] = make_float2(pj.x, pj.y);
     uint4* const slab = reinterpret_cast<uint4*>(G.vlist) + k;  // group g at slab[g * n]
     uint4 buf = make_uint4(kVlNone, kVlNone, kVlNone, kVlNone);
@@ -569,21 +570,6 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_vl_build(DevParams P, Sta
         atomicOr(S.vl_rebuild, 1u);
         atomicOr(S.vl_gone, 2u);
     }
-}
-
-// Steps that reuse the lists: cell-order copies, positions relative to each
-// particle's build cell (the key pass left the current cell and offset).
-__global__ void k_vl_reorder(DevParams P, State S, Sorted G) {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= P.n) return;
-    const uint32_t id = G.id[k], key = G.key[k];
-    const uint32_t now = S.cxy[id];
-    const float2 o = S.coff2[id];
-    const float ox = o.x + (float)((int)(now & 0xFFFFu) - (int)second_bits(key)) * P.mf.cell;
-    const float oy = o.y + (float)((int)(now >> 16) - (int)second_bits(key >> 1)) * P.mf.cell;
-    G.P4[k] = make_float4(ox, oy, 0.0f, __int_as_float(S.itype[id]));
-    const float2 v = S.vpf2[id];
-    G.V4[k] = make_float4(v.x, v.y, 0.0f, 0.0f);  // .w: the density pass writes it
 }
 
 // Stencil offset of a list entry's 5-bit cell code (dx + 2) * 5 + (dy + 2):
@@ -840,9 +826,6 @@ void launch_verlet_upload_check(uint32_t* rebuild, const uint32_t* gone, cudaStr
 void launch_verlet_build(const DevParams& P, const State& S, const Sorted& G, cudaStream_t st) {
     constexpr int kBuildThreads = 128;
     k_vl_build<<<(P.n + kBuildThreads - 1) / kBuildThreads, kBuildThreads, 0, st>>>(P, S, G);
-}
-void launch_verlet_reorder(const DevParams& P, const State& S, const Sorted& G, cudaStream_t st) {
-    k_vl_reorder<<<(P.n + 255) / 256, 256, 0, st>>>(P, S, G);
 }
 void launch_density_verlet(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
                            cudaStream_t st, int threads) {

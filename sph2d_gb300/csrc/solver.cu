@@ -193,8 +193,9 @@ void set_verlet_params(rrsph_solver* s) {
     s->P.vl_cut2 = (float)(c * c * (1.0 + 1e-4));
     s->P.vl_half_skin2 = (float)(0.25 * skin * skin * (1.0 - 1e-4));
     s->P.vl_skin_edge = (float)(skin * 1.01);
-    // reset + sort (3 per 8-bit pass) + reorder + build, against the reuse copy's 1
-    s->vl_extra_launches = 2ull + 3ull * (unsigned long long)((s->sort_bits + 7) / 8);
+    // reset + sort (3 per 8-bit pass) + reorder + build (a step that reuses the
+    // lists launches nothing for them: the key pass wrote its cell-order copies)
+    s->vl_extra_launches = 3ull + 3ull * (unsigned long long)((s->sort_bits + 7) / 8);
 }
 
 int check_handle(rrsph_solver* s, const char* fn) {
@@ -236,10 +237,10 @@ void enqueue_forces(rrsph_solver* s, uint32_t terms, rrsph::StepScalars* scal, i
 // phases. with_keys runs the predict + key pass first; otherwise the previous
 // step's whole-step kernel has done it. The whole-step kernel always prepares
 // the next step's predict + keys.
-// Neighbour reuse: the grid + list rebuild, or the cell-order copies of a
-// step that reuses the lists, on stream st. The rebuilt grid stays in
-// (keys_a, ids_a) while the lists are reused: the key pass of every step
-// rewrites keys_in.
+// Neighbour reuse: the grid + list rebuild on stream st (a step that reuses
+// the lists has its cell-order copies from the key pass). The rebuilt grid
+// stays in (keys_a, ids_a) while the lists are reused: the key pass of every
+// step rewrites keys_in.
 void enqueue_verlet_rebuild(rrsph_solver* s, cudaStream_t st) {
     rrsph::launch_verlet_reset(s->S.vl_rebuild, s->S.vl_gone, s->vl_builds, st);
     rrsph::radix_sort_pairs_into(s->G.keys_in, s->G.ids_in, s->G.keys_a, s->G.ids_a, s->G.keys_b, s->G.ids_b,
@@ -251,14 +252,10 @@ void enqueue_verlet_rebuild(rrsph_solver* s, cudaStream_t st) {
     rrsph::launch_verlet_build(s->P, s->S, s->G, st);
     s->launches += 3;
 }
-void enqueue_verlet_reuse(rrsph_solver* s, cudaStream_t st) {
-    rrsph::launch_verlet_reorder(s->P, s->S, s->G, st);
-    s->launches++;
-}
 
 // One step of the 2D mixed loop with neighbour reuse. In a captured graph the
-// rebuild / reuse choice is a conditional node that a kernel sets from the flag
-// the last key pass raised; with direct launches the host reads the flag.
+// rebuild is a conditional node that a kernel sets from the flag the last key
+// pass raised; with direct launches the host reads the flag.
 int enqueue_step_verlet(rrsph_solver* s, int par, cudaEvent_t* events, bool with_keys) {
     rrsph::StepScalars* cur = s->scal + par;
     rrsph::StepScalars* nxt = s->scal + (par ^ 1);
@@ -287,11 +284,10 @@ int enqueue_step_verlet(rrsph_solver* s, int par, cudaEvent_t* events, bool with
         np.type = cudaGraphNodeTypeConditional;
         np.conditional.handle = h;
         np.conditional.type = cudaGraphCondTypeIf;
-        np.conditional.size = 2;
+        np.conditional.size = 1;
         cudaGraphNode_t cnode;
         RRSPH_CUDA_TRY(cudaGraphAddNode(&cnode, g, deps, nullptr, nd, &np));
-        s->vl_body[0] = np.conditional.phGraph_out[0];
-        s->vl_body[1] = np.conditional.phGraph_out[1];
+        s->vl_body = np.conditional.phGraph_out[0];
         s->vl_pending = true;
         RRSPH_CUDA_TRY(cudaStreamUpdateCaptureDependencies(st, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
     } else {
@@ -300,9 +296,7 @@ int enqueue_step_verlet(rrsph_solver* s, int par, cudaEvent_t* events, bool with
         if (*s->h_vl) {
             const unsigned long long before = s->launches;
             enqueue_verlet_rebuild(s, st);
-            s->launches = before + 1;  // a rebuild's extra launches are counted from vl_builds
-        } else {
-            enqueue_verlet_reuse(s, st);
+            s->launches = before;  // a rebuild's launches are counted from vl_builds
         }
     }
     if (events) {
@@ -319,23 +313,17 @@ int enqueue_step_verlet(rrsph_solver* s, int par, cudaEvent_t* events, bool with
     return RRSPH_OK;
 }
 
-// Fills the bodies of the conditional node of a just-captured reuse step;
-// *reuse_launches gets the launches of the reuse body.
-int capture_verlet_bodies(rrsph_solver* s, unsigned long long* reuse_launches) {
+// Fills the rebuild body of the conditional node of a just-captured step (its
+// launches are counted from vl_builds).
+int capture_verlet_body(rrsph_solver* s) {
     s->vl_pending = false;
-    unsigned long long counts[2] = {0, 0};
-    for (int b = 0; b < 2; b++) {
-        const unsigned long long before = s->launches;
-        RRSPH_CUDA_TRY(cudaStreamBeginCaptureToGraph(s->aux, s->vl_body[b], nullptr, nullptr, 0,
-                                                     cudaStreamCaptureModeThreadLocal));
-        if (b == 0) enqueue_verlet_rebuild(s, s->aux);
-        else enqueue_verlet_reuse(s, s->aux);
-        cudaGraph_t out = nullptr;
-        RRSPH_CUDA_TRY(cudaStreamEndCapture(s->aux, &out));
-        counts[b] = s->launches - before;
-        s->launches = before;
-    }
-    *reuse_launches = counts[1];
+    const unsigned long long before = s->launches;
+    RRSPH_CUDA_TRY(cudaStreamBeginCaptureToGraph(s->aux, s->vl_body, nullptr, nullptr, 0,
+                                                 cudaStreamCaptureModeThreadLocal));
+    enqueue_verlet_rebuild(s, s->aux);
+    cudaGraph_t out = nullptr;
+    RRSPH_CUDA_TRY(cudaStreamEndCapture(s->aux, &out));
+    s->launches = before;
     return RRSPH_OK;
 }
 
@@ -465,7 +453,7 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
     } else {
         if (d3) { A(S.coff4, n); A(S.vpf4, n); } else { A(S.coff2, n); A(S.vpf2, n); }
         if (!d3 && !cont) {  // neighbour reuse
-            A(S.cxy, n); A(S.bcxy, n); A(S.boff, n); A(S.vl_rebuild, 2); A(s->vl_builds, 1);
+            A(S.cxy, n); A(S.bcxy, n); A(S.slot, n); A(S.boff, n); A(S.vl_rebuild, 2); A(s->vl_builds, 1);
             S.vl_gone = S.vl_rebuild + 1;
             A(G.vlist, (size_t)rrsph::kVerletCap * n); A(G.vcount, n); A(G.nlist, (size_t)rrsph::kVerletCap * n); A(G.ncount, n);
             A(G.keys_b, n); A(G.ids_b, n);
@@ -488,6 +476,7 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
             cudaMemsetAsync(G.vcount, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
             cudaMemsetAsync(G.ncount, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
             cudaMemsetAsync(S.bcxy, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
+            cudaMemsetAsync(S.slot, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
             cudaMemsetAsync(S.boff, 0, n * sizeof(float2), s->stream) != cudaSuccess ||
             cudaMemsetAsync(G.keys_a, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
             cudaMemsetAsync(G.ids_a, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess)
@@ -636,9 +625,8 @@ int enqueue_steps(rrsph_solver* s, uint64_t nsteps) {
                 }
                 if (ce != cudaSuccess)
                     return set_error(RRSPH_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ce));
-                unsigned long long body = 0;
                 if (s->vl_pending) {
-                    const int rb = capture_verlet_bodies(s, &body);
+                    const int rb = capture_verlet_body(s);
                     if (rb) {
                         cudaGraphDestroy(g);
                         return rb;
@@ -647,7 +635,7 @@ int enqueue_steps(rrsph_solver* s, uint64_t nsteps) {
                 const cudaError_t e = cudaGraphInstantiate(&s->graph[par], g, 0);
                 cudaGraphDestroy(g);
                 if (e != cudaSuccess) return set_error(RRSPH_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
-                s->launches_in_graph[par] = s->launches - before + body;
+                s->launches_in_graph[par] = s->launches - before;
                 s->launches = before;
             }
             if (with_keys) enqueue_keys_dim(s, par);

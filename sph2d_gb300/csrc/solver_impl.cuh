@@ -55,7 +55,7 @@ struct rrsph_solver {
     cudaStream_t aux = nullptr;                // captures the rebuild / reuse bodies of a step graph
     unsigned long long* vl_builds = nullptr;   // device: list builds since creation
     uint32_t* h_vl = nullptr;                  // pinned: the rebuild flag, read with direct launches
-    cudaGraph_t vl_body[2] = {nullptr, nullptr};  // bodies of the graph being captured (rebuild, reuse)
+    cudaGraph_t vl_body = nullptr;  // rebuild body of the graph being captured
     bool vl_pending = false;
     unsigned long long vl_extra_launches = 0;  // launches a rebuild adds to a reuse step
 };
