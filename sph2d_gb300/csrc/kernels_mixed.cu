@@ -614,16 +614,19 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
                 const uint4* slab = reinterpret_cast<const uint4*>(G.vlist) + k;  // group g at slab[g * n]
                 // shift of stencil offset (cx, cy) = (cx - 2, cy - 2) cells, relative to this particle
                 const float bx = -2.0f * M.cell - pj.x, by = -2.0f * M.cell - pj.y;
-                // groups of four entries (one load), then their particles, loaded together;
-                // the body has no branch but the rare guard-band test, and every term
-                // is added with compensation
+                // groups of four entries (one load, the next group's issued before this
+                // one's particles are loaded), then their particles, loaded together;
+                // the body has no branch but the rare guard-band test, and each group's
+                // sum is added with compensation
+                uint4 w = vc ? slab[0] : make_uint4(kVlNone, kVlNone, kVlNone, kVlNone);
                 for (uint32_t e0 = 0; e0 < vc; e0 += kVlBatch) {
-                    const uint4 w = slab[(size_t)(e0 >> 2) * P.n];
+                    const uint4 wn = e0 + kVlBatch < vc ? slab[(size_t)((e0 >> 2) + 1) * P.n] : w;
                     const uint32_t en[kVlBatch] = {w.x, w.y, w.z, w.w};
                     float4 pb[kVlBatch];
 #pragma unroll
                     for (int j = 0; j < kVlBatch; j++)
                         pb[j] = en[j] != kVlNone ? G.P4[en[j] & 0x07FFFFFFu] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    float part = 0.0f;
 #pragma unroll
                     for (int j = 0; j < kVlBatch; j++) {
                         uint32_t cx, cy;
@@ -636,10 +639,12 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
                         if (in && !(d2 < M.cut2_lo)) in = within_cutoff<2>(P, S, G, en[j] & 0x07FFFFFFu, k, d2);
                         const float q = d2 * rsqrtf(d2) * M.inv_h;
                         const float wv = SKF == 1 ? cubic_wf_sel(f, q) : kernel_wf(skf, f, q);
-                        acc.add(in ? M.mass * wv : 0.0f);
+                        part += in ? wv : 0.0f;
                         if (in) nslab[(size_t)(cnt >> 2) * 4 * P.n + (cnt & 3u)] = en[j];
                         cnt += in;
                     }
+                    acc.add(M.mass * part);
+                    w = wn;
                 }
             } else {
                 const Stencil<2> st(P, G.key[k]);
