@@ -55,6 +55,10 @@ struct Sorted {
     float4* V4;    // velocity the forces use + density the forces use
     float4* VD4;   // v + (rho - rho0) for density_con
     float2* PR;    // pressure p and p / rho^2 (rho = the density the forces use)
+    // 2D mixed step with neighbour reuse: the P4 / V4 of the next step, which the
+    // key pass writes at each particle's build slot (the two buffers alternate)
+    float4* P4n;
+    float4* V4n;
     // 2D mixed step: neighbour masks written by the density pass for the force
     // pass, SoA [10][n]: word c < 9 = bit b set if particle cell_start + b of
     // stencil cell c is a neighbour; word 9 = stencil cells with more than 32
@@ -117,8 +121,11 @@ void launch_verlet_upload_check(uint32_t* rebuild, const uint32_t* gone, cudaStr
 void launch_verlet_build(const DevParams& P, const State& S, const Sorted& G, cudaStream_t st);
 void launch_density_verlet(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
                            cudaStream_t st, int threads);
-void launch_forces_verlet(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
-                          cudaStream_t st, int threads);
+// whole != 0: the whole step of each particle (launch_whole_step with next keys)
+// runs in the force gather's thread; needs dt without the step's reduction and
+// at most kVerletCap + 1 neighbours per particle (max_nb).
+void launch_forces_verlet(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal,
+                          StepScalars* scal_next, uint32_t* flags, cudaStream_t st, int threads, int whole);
 
 void launch_cells_start(const DevParams& P, const Sorted& G, uint32_t* out, cudaStream_t st);
 template <int DIM>

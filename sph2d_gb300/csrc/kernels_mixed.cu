@@ -14,6 +14,7 @@
 // reciprocals and square roots use the fast MUFU forms (<= 2 ulp).
 #include "kernels.cuh"
 #include "neighbour.cuh"
+#include "step_particle.cuh"
 
 namespace rrsph {
 
@@ -666,6 +667,10 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
                         const float dx = pi.x + shx, dy = pi.y + shy;
                         const float d2 = dx * dx + dy * dy;
                         if (!within_cutoff<2>(P, S, G, i, k, d2)) continue;
+                        // this step's neighbour list too (the grid is this step's: code of (sx, sy))
+                        if (cnt < (uint32_t)kVerletCap)
+                            nslab[(size_t)(cnt >> 2) * 4 * P.n + (cnt & 3u)] =
+                                i | ((uint32_t)((sx + 2) * 5 + (sy + 2)) << 27);
                         cnt++;
                         part += kernel_wf(skf, f, d2 * rsqrtf(d2) * M.inv_h);
                     }
@@ -673,7 +678,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
                 }
             }
         }
-        G.ncount[k] = G.vcount[k] != kListOver ? cnt : 0u;
+        G.ncount[k] = cnt < (uint32_t)kVerletCap ? cnt : (uint32_t)kVerletCap;
         if (cnt > P.max_nb - 1) atomicOr(flags, RRSPH_FLAG_NEIGHBOUR_OVERFLOW);
         const float d = ((acc.s - M.rho0_minus_w0_hi) - acc.c) - M.rho0_minus_w0_lo;
         const float rho = M.rho0 + d;
@@ -688,15 +693,21 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
     warp_sum_add(&scal->pairs, cnt);
 }
 
-// update_acceleration over this step's neighbours: the list entries the
-// density pass marked (or the stencil search for an overflowed list). A
-// neighbour's pressure comes with its velocity and density (V4.z). STD: the
-// common method set of ForceAcc::pair_std, fixed at compile time. At most 64
-// registers (4 blocks of 256 threads per SM): the gather hides its L1/L2
-// latency with warps.
-template <int SKF, bool STD>
+// update_acceleration over this step's neighbours: the list the density pass
+// wrote (or the stencil search for an overflowed list). A neighbour's pressure
+// comes with its velocity and density (V4.z). STD: the common method set of
+// ForceAcc::pair_std, fixed at compile time. At most 64 registers (4 blocks of
+// 256 threads per SM): the gather hides its L1/L2 latency with warps.
+// WV != 0: the whole step follows in the same thread (whole_particle with
+// variant WV, thread 0 advancing the scalars into next): it reads nothing that
+// another thread's whole step writes, because this step's copies (P4, V4) are
+// not the ones the key pass writes (P4n, V4n), and the list of every particle
+// is complete (the density pass wrote the neighbours of overflowed lists too,
+// which needs at most kVerletCap neighbours per particle).
+template <int SKF, bool STD, int WV>
 __global__ void __launch_bounds__(kMaxGatherThreads, 4) k_forces_verlet(DevParams P, State S, Sorted G,
                                                                     StepScalars* __restrict__ scal,
+                                                                    StepScalars* __restrict__ next,
                                                                     uint32_t* __restrict__ flags) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = k < P.n;
@@ -720,7 +731,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads, 4) k_forces_verlet(DevParam
         Kahan avx{0, 0}, avy{0, 0};
         if (tj != P.type_non_existent) {
             const uint32_t vc = G.vcount[k];
-            if (vc != kListOver) {
+            if (WV != 0 || vc != kListOver) {
                 // this step's neighbours, four list words per load (the lanes of a
                 // warp load neighbouring uint4s), their data two at a time
                 const uint32_t nc = G.ncount[k];
@@ -810,6 +821,11 @@ __global__ void __launch_bounds__(kMaxGatherThreads, 4) k_forces_verlet(DevParam
         }
         arvmu_d = F.arvmu;
         if (P.dt_reduce) amag = sqrt(axd * axd + ayd * ayd);
+        if (WV != 0) {
+            const double dt = step_dt<(WV & kVarRare) != 0>(P, scal, flags, k == 0);
+            if (k == 0) advance_scalars(P, scal, next, dt);
+            whole_particle<2, WV>(P, S, G, id, dt, scal, flags, 1, axd, ayd, 0.0);
+        }
     }
     if (P.dt_method == 2 && P.dt_reduce) {
         warp_max_bits(&scal->amax_bits, amag);
@@ -838,13 +854,23 @@ void launch_density_verlet(const DevParams& P, const State& S, const Sorted& G, 
     if (P.all_cubic) k_density_verlet<1><<<blocks, threads, 0, st>>>(P, S, G, scal, flags);
     else k_density_verlet<0><<<blocks, threads, 0, st>>>(P, S, G, scal, flags);
 }
-void launch_forces_verlet(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
-                          cudaStream_t st, int threads) {
+void launch_forces_verlet(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal,
+                          StepScalars* scal_next, uint32_t* flags, cudaStream_t st, int threads, int whole) {
     const unsigned blocks = (P.n + threads - 1) / threads;
     const bool std_terms = P.all_cubic && P.intf_form != 1 && P.art_visc && !P.art_pressure && !P.avg_vel;
-    if (std_terms) k_forces_verlet<1, true><<<blocks, threads, 0, st>>>(P, S, G, scal, flags);
-    else if (P.all_cubic) k_forces_verlet<1, false><<<blocks, threads, 0, st>>>(P, S, G, scal, flags);
-    else k_forces_verlet<0, false><<<blocks, threads, 0, st>>>(P, S, G, scal, flags);
+    const int wv = whole ? (kVarMixed | (P.avg_vel || P.dt_method == 2 ? kVarRare : 0)) : 0;
+#define RRSPH_FV(SKF, STD)                                                                                      \
+    do {                                                                                                        \
+        if (wv == 0) k_forces_verlet<SKF, STD, 0><<<blocks, threads, 0, st>>>(P, S, G, scal, scal_next, flags);  \
+        else if (wv == kVarMixed)                                                                               \
+            k_forces_verlet<SKF, STD, kVarMixed><<<blocks, threads, 0, st>>>(P, S, G, scal, scal_next, flags);  \
+        else k_forces_verlet<SKF, STD, kVarMixed | kVarRare><<<blocks, threads, 0, st>>>(P, S, G, scal, scal_next, \
+                                                                                          flags);               \
+    } while (0)
+    if (std_terms) RRSPH_FV(1, true);
+    else if (P.all_cubic) RRSPH_FV(1, false);
+    else RRSPH_FV(0, false);
+#undef RRSPH_FV
 }
 
 template <int DIM>

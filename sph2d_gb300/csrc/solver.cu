@@ -241,6 +241,15 @@ void enqueue_forces(rrsph_solver* s, uint32_t terms, rrsph::StepScalars* scal, i
 // the lists has its cell-order copies from the key pass). The rebuilt grid
 // stays in (keys_a, ids_a) while the lists are reused: the key pass of every
 // step rewrites keys_in.
+// Neighbour reuse: the step of parity `read` reads P4 / V4 [read]; the key
+// pass writes its copies into [write].
+void set_verlet_copies(rrsph_solver* s, int read, int write) {
+    s->G.P4 = s->p4buf[read];
+    s->G.V4 = s->v4buf[read];
+    s->G.P4n = s->p4buf[write];
+    s->G.V4n = s->v4buf[write];
+}
+
 void enqueue_verlet_rebuild(rrsph_solver* s, cudaStream_t st) {
     rrsph::launch_verlet_reset(s->S.vl_rebuild, s->S.vl_gone, s->vl_builds, st);
     rrsph::radix_sort_pairs_into(s->G.keys_in, s->G.ids_in, s->G.keys_a, s->G.ids_a, s->G.keys_b, s->G.ids_b,
@@ -263,10 +272,12 @@ int enqueue_step_verlet(rrsph_solver* s, int par, cudaEvent_t* events, bool with
     s->G.key = s->G.keys_a;  // the grid of the last rebuild
     s->G.id = s->G.ids_a;
     if (events) cudaEventRecord(events[0], st);
+    if (with_keys) set_verlet_copies(s, par, par);  // this step's copies from its own key pass
     if (with_keys) {
         rrsph::launch_keys<2>(s->P, s->S, s->G, cur, 1, s->flags, st);
         s->launches++;
     }
+    set_verlet_copies(s, par, par ^ 1);
     if (events) cudaEventRecord(events[1], st);
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     RRSPH_CUDA_TRY(cudaStreamIsCapturing(st, &cs));
@@ -305,11 +316,14 @@ int enqueue_step_verlet(rrsph_solver* s, int par, cudaEvent_t* events, bool with
     }
     rrsph::launch_density_verlet(s->P, s->S, s->G, cur, s->flags, st, s->gather_threads[0]);
     if (events) cudaEventRecord(events[4], st);
-    rrsph::launch_forces_verlet(s->P, s->S, s->G, cur, s->flags, st, s->gather_threads[1]);
+    // the whole step runs inside the force gather unless dt waits for the step's
+    // maxima or a particle may have more neighbours than a list holds
+    const bool fuse = !(s->P.dt_method == 2 && s->P.dt_reduce) && s->P.max_nb <= rrsph::kVerletCap + 1;
+    rrsph::launch_forces_verlet(s->P, s->S, s->G, cur, nxt, s->flags, st, s->gather_threads[1], fuse ? 1 : 0);
     if (events) cudaEventRecord(events[5], st);
-    rrsph::launch_whole_step<2>(s->P, s->S, s->G, cur, nxt, s->flags, 1, st);
+    if (!fuse) rrsph::launch_whole_step<2>(s->P, s->S, s->G, cur, nxt, s->flags, 1, st);
     if (events) cudaEventRecord(events[6], st);
-    s->launches += 3;
+    s->launches += fuse ? 2 : 3;
     return RRSPH_OK;
 }
 
@@ -361,6 +375,7 @@ int enqueue_step_dim(rrsph_solver* s, int par, cudaEvent_t* events, bool with_ke
 }
 
 void enqueue_keys_dim(rrsph_solver* s, int par) {
+    if (s->verlet) set_verlet_copies(s, par, par);
     if (s->dim == 3) rrsph::launch_keys<3>(s->P, s->S, s->G, s->scal + par, 1, s->flags, s->stream);
     else rrsph::launch_keys<2>(s->P, s->S, s->G, s->scal + par, 1, s->flags, s->stream);
     s->launches++;
@@ -459,6 +474,11 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
             A(G.keys_b, n); A(G.ids_b, n);
         }
         A(G.P4, n); A(G.V4, n); A(G.PR, n);
+        s->p4buf[0] = s->p4buf[1] = G.P4;
+        s->v4buf[0] = s->v4buf[1] = G.V4;
+        if (G.vlist) { A(s->p4buf[1], n); A(s->v4buf[1], n); }
+        G.P4n = s->p4buf[1];
+        G.V4n = s->v4buf[1];
         if (!d3) A(G.nbmask, 10 * n);
         if (cont) A(G.VD4, n);
     }
