@@ -40,14 +40,18 @@ METRIC = "pair-interactions/s and ms/step: FP32-mixed vs FP64 GPU step at stated
 UNIT = "pair-interactions/s"
 L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
 
-# Algorithmic bytes of the dominant kernel (the force gather, k_forces_verlet)
-# of the FP32-mixed 2D step with neighbour reuse: per particle it reads its id 4,
-# position+type float4 16, velocity+pressure+density float4 16, (p, p/rho^2)
-# float2 8, candidate count 4 and neighbour count 4, and writes a.x, a.y as
-# double 16; per neighbour pair it reads one 4-byte word of this step's
+# Algorithmic bytes of the dominant kernel, k_forces_verlet of the FP32-mixed
+# 2D step with neighbour reuse: the force gather with the whole step fused in.
+# Per particle, the gather reads id 4, position+type float4 16,
+# velocity+pressure+density float4 16, (p, p/rho^2) float2 8, candidate and
+# neighbour counts 4 + 4 and writes a.x, a.y doubles 16; the whole step reads
+# r, v doubles 32, itype 4, key_of 4, build cell 4, build offset 8, build slot 4
+# and writes r, v 32, v_predict float2 8, cell offset float2 8, cell 4, key_of
+# 4, sort key + id 8, the next step's position and velocity float4s 32 and one
+# cell-table word 4. Per neighbour pair it reads one 4-byte word of this step's
 # neighbour list. The neighbours' own data are re-reads of particles other
 # threads load (L1/L2), not algorithmic bytes.
-FORCES_REUSE_BYTES_PER_PARTICLE = 4 + 16 + 16 + 8 + 4 + 4 + 16
+FORCES_REUSE_BYTES_PER_PARTICLE = (52 + 16) + (32 + 4 + 4 + 4 + 8 + 4) + (32 + 8 + 8 + 4 + 4 + 8 + 32 + 4)
 FORCES_REUSE_BYTES_PER_PAIR = 4
 FORCES_FP64_BYTES_PER_PARTICLE_2D = 4 + 4 + 16 + 4 + 16 + 8 + 8 + 16
 
@@ -307,7 +311,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         "phases_ms_per_step": phases_mixed,
         "roofline": {
             "bound": "hbm",
-            "kernel": "k_forces_verlet",
+            "kernel": "k_forces_verlet (force gather + whole step)",
             "achieved": achieved,
             "peak": hbm_peak,
             "unit": "GB/s",
