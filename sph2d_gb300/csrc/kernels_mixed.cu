@@ -619,9 +619,10 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
                 // one's particles are loaded), then their particles, loaded together;
                 // the body has no branch but the rare guard-band test, and each group's
                 // sum is added with compensation
-                uint4 w = vc ? slab[0] : make_uint4(kVlNone, kVlNone, kVlNone, kVlNone);
+                // (list words are read once a step: streaming loads keep L1 for the neighbours' data)
+                uint4 w = vc ? __ldcs(slab) : make_uint4(kVlNone, kVlNone, kVlNone, kVlNone);
                 for (uint32_t e0 = 0; e0 < vc; e0 += kVlBatch) {
-                    const uint4 wn = e0 + kVlBatch < vc ? slab[(size_t)((e0 >> 2) + 1) * P.n] : w;
+                    const uint4 wn = e0 + kVlBatch < vc ? __ldcs(slab + (size_t)((e0 >> 2) + 1) * P.n) : w;
                     const uint32_t en[kVlBatch] = {w.x, w.y, w.z, w.w};
                     float4 pb[kVlBatch];
 #pragma unroll
@@ -738,7 +739,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads, 4) k_forces_verlet(DevParam
                 const uint4* nslab = reinterpret_cast<const uint4*>(G.nlist) + k;  // group g at nslab[g * n]
                 const float bx = -2.0f * M.cell - pj4.x, by = -2.0f * M.cell - pj4.y;
                 for (uint32_t e0 = 0; e0 < nc; e0 += 4) {
-                    const uint4 w = nslab[(size_t)(e0 >> 2) * P.n];
+                    const uint4 w = __ldcs(nslab + (size_t)(e0 >> 2) * P.n);  // streaming, as in the density pass
                     const uint32_t eg[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
                     for (int h = 0; h < 4; h += kVlForceBatch) {
