@@ -332,6 +332,8 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     s64.close()
     if rank == 0 and world == 1 and not args.no_ensemble:
         result["ensemble"] = ensemble_measure()
+    if rank == 0 and world == 1 and not args.no_dam3d:
+        result["dam_break_3d"] = dam3d_measure()
     if rank == 0 and world == 1 and not args.no_adjoint:
         result["adjoint"] = adjoint_measure(steps=args.adjoint_steps)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -403,6 +405,58 @@ def ensemble_measure(steps: int = 50, seq_steps: int = 10, ntanks: int = 256) ->
         "sequential": {"ms_per_step": seq_ms, "pair_interactions_per_s": seq_rate, "steps_per_tank": seq_steps},
         "speedup": seq_ms / (ms / steps),
         "launches_in_batched_region": launches,
+    }
+
+
+def dam3d_measure(steps: int = 5, fp64_steps: int = 2) -> dict:
+    """The 3D dam break at full size: the FP32-mixed step against the plain
+    FP64 GPU step on the same uploaded state (each timed with CUDA events on its
+    solver's stream over graph replays; the working set is gigabytes, far
+    beyond the L2), and the mixed state's relative L2 error against the FP64
+    step's after 1 and `steps` steps."""
+    import torch
+
+    from sph2d_gb300 import Solver, cases
+
+    case = cases.dam_break_3d()
+    p = case.params()
+    out = {}
+    states = {}
+    for prec, n in (("mixed", steps), ("fp64", fp64_steps)):
+        with Solver(p, prec) as s:
+            s.upload(case.r, case.v, case.rho, case.itype)
+            s.step(1, 0.0)
+            states[(prec, 1)] = s.download()
+            if prec == "mixed":
+                s.step(steps - 1, 0.0)
+                states[(prec, steps)] = s.download()
+            s.upload(case.r, case.v, case.rho, case.itype)
+            s.step_async(1)
+            s.sync()
+            _, q0 = s.pair_count()
+            ext = torch.cuda.ExternalStream(s.stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            s.step_async(n)
+            e1.record(ext)
+            s.sync()
+            ms = e0.elapsed_time(e1) / n
+            _, q1 = s.pair_count()
+            out[prec] = {"ms_per_step": ms, "pair_interactions_per_s": (q1 - q0) / n / (ms / 1e3), "steps": n,
+                         "pairs_per_step": (q1 - q0) / n}
+    with Solver(p, "fp64") as s:  # the FP64 reference state after `steps` steps
+        s.upload(case.r, case.v, case.rho, case.itype)
+        s.step(steps, 0.0)
+        states[("fp64", steps)] = s.download()
+    err = {f"after_{k}_steps": {f: _rel(states[("mixed", k)][f], states[("fp64", k)][f]) for f in ("r", "v", "rho", "p")}
+           for k in (1, steps)}
+    return {
+        "workload": f"3D dam break: tank 1.6 x 0.67 x 0.6 m, block 0.4 x 0.67 x 0.3 m at dx 2.6 mm, h 1.3 dx, "
+                    f"LJ walls at dx/2, continuity density; {case.ntotal} particles ({int(case.notes['nfluid'])} fluid)",
+        "mixed": out["mixed"], "fp64": out["fp64"],
+        "mixed_speedup": out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"],
+        "error_vs_fp64_gpu": dict(err, metric="relative L2"),
+        "timing": "inputs larger than L2 (no flush)",
     }
 
 
@@ -538,6 +592,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 256-tank ensemble measurement")
+    ap.add_argument("--no-dam3d", action="store_true", help="skip the 3D dam break measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost measurement")
     ap.add_argument("--adjoint-steps", type=int, default=500)
     args = ap.parse_args()
