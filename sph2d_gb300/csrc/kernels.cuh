@@ -135,8 +135,26 @@ template <int DIM>
 void launch_unpack(const DevParams& P, State S, const double* r, const double* v, uint32_t stride, cudaStream_t st);
 template <int DIM>
 void launch_pack(const DevParams& P, State S, double* r, double* v, uint32_t stride, cudaStream_t st);
+// The time of the next step (and flags cleared, when non-null); after steps,
+// the time and flags into a mapped host mailbox (device address `out`).
+struct HostReport {
+    double time;
+    uint32_t flags;
+};
+void launch_set_time(StepScalars* scal, double time, uint32_t* flags, cudaStream_t st);
+void launch_report(const StepScalars* scal, const uint32_t* flags, HostReport* out, cudaStream_t st);
+// Upload / download through device-addressable host arrays (pinned memory):
+// one kernel reading (writing) the caller's arrays over the host link. The
+// upload also runs the first step's predict + key pass (launch_keys).
+template <int DIM>
+void launch_upload_direct(const DevParams& P, const State& S, const Sorted& G, const double* r, const double* v,
+                          const double* rho, const double* p, const int32_t* itype, uint32_t stride,
+                          StepScalars* scal, double dt, uint32_t* flags, cudaStream_t st);
+template <int DIM>
+void launch_download_direct(const DevParams& P, const State& S, double* r, double* v, double* rho, double* p,
+                            int32_t* itype, uint32_t stride, cudaStream_t st);
 
-constexpr int kVerletCap = 64;          // candidate-list entries per particle (one 64-bit mask)
+constexpr int kVerletCap = 64;          // candidate-list entries per particle
 constexpr uint32_t kListOver = 0xFFFFFFFFu;
 constexpr uint32_t kVlNone = 0xFFFFFFFFu;  // padding of a list row (never an entry)
 constexpr int kGatherThreads = 128;     // default block size of the pair gathers

@@ -193,7 +193,143 @@ __global__ void k_pack(DevParams P, State S, double* __restrict__ r, double* __r
     }
 }
 
+// A coordinate triple (x, y[, z]) of a strided host array: 16-byte loads and
+// stores where the layout allows (stride 2 in 2D, stride 4 in 3D, 16-byte
+// aligned), since partial-line accesses over the host link are slow. A
+// stride-4 store also writes 0 into the pad.
+template <int DIM>
+__device__ __forceinline__ void host_read3(const double* __restrict__ a, size_t b, bool vec, double& x, double& y,
+                                           double& z) {
+    if (vec) {
+        const double2 q = *reinterpret_cast<const double2*>(a + b);
+        x = q.x;
+        y = q.y;
+        if (DIM == 3) z = *(a + b + 2);
+    } else {
+        x = a[b];
+        y = a[b + 1];
+        if (DIM == 3) z = a[b + 2];
+    }
+}
+template <int DIM>
+__device__ __forceinline__ void host_write3(double* __restrict__ a, size_t b, bool vec, double x, double y,
+                                            double z) {
+    if (vec) {
+        reinterpret_cast<double2*>(a + b)[0] = make_double2(x, y);
+        if (DIM == 3) reinterpret_cast<double2*>(a + b)[1] = make_double2(z, 0.0);
+    } else {
+        a[b] = x;
+        a[b + 1] = y;
+        if (DIM == 3) a[b + 2] = z;
+    }
+}
+
+// rrsph_upload from host arrays the device can address (page-locked host
+// memory): the state straight from the caller's arrays over the host link, the
+// fresh work arrays of time_integration (TimeIntegration.cpp:35-50) zeroed,
+// (thread 0) the step scalars of step 0, then the first step's predict + key
+// pass of k_keys (zero acceleration, dt of step 0) while the link is still
+// busy. The neighbour-list check of an upload runs before this kernel: its
+// key pass may raise the rebuild flag, which the check resets.
+template <int DIM>
+__global__ void k_upload_direct(DevParams P, State S, Sorted G, const double* __restrict__ r,
+                                const double* __restrict__ v, const double* __restrict__ rho,
+                                const double* __restrict__ p, const int32_t* __restrict__ itype, uint32_t stride,
+                                int vec, StepScalars* __restrict__ scal, double dt, uint32_t* __restrict__ flags) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        *scal = StepScalars{};
+        scal->dt = dt;
+    }
+    if (i >= P.n) return;
+    const size_t b = (size_t)i * stride;
+    double x, y, z = 0.0;
+    host_read3<DIM>(r, b, vec, x, y, z);
+    S.rx[i] = x;
+    S.ry[i] = y;
+    if (DIM == 3) S.rz[i] = z;
+    host_read3<DIM>(v, b, vec, x, y, z);
+    S.vx[i] = x;
+    S.vy[i] = y;
+    if (DIM == 3) {
+        S.vz[i] = z;
+        S.az[i] = 0.0;
+    }
+    const double rh = rho[i];
+    S.rho[i] = rh;
+    S.p[i] = p ? p[i] : 0.0;
+    S.itype[i] = itype[i];
+    S.ax[i] = 0.0;
+    S.ay[i] = 0.0;
+    if (S.avx) {
+        S.avx[i] = 0.0;
+        S.avy[i] = 0.0;
+        if (DIM == 3) S.avz[i] = 0.0;
+    }
+    S.drho[i] = 0.0;
+    const double vx = S.vx[i], vy = S.vy[i], vz = DIM == 3 ? S.vz[i] : 0.0;
+    if (P.density_treatment) predict<DIM, 2, true>(P, S, i, vx, vy, vz, rh, dt, 0.0, 0.0, 0.0);
+    else predict<DIM, 2, false>(P, S, i, vx, vy, vz, 0.0, dt, 0.0, 0.0, 0.0);
+    key_pass<DIM, 2>(P, S, G, i, S.rx[i], S.ry[i], DIM == 3 ? S.rz[i] : 0.0, flags);
+}
+
+// rrsph_step's bookkeeping as kernels on the stream (no copy-engine round
+// trips): the time of the next step (and cleared status flags) before the
+// steps, the time and flags after them into a host mailbox.
+__global__ void k_set_time(StepScalars* __restrict__ scal, double time, uint32_t* __restrict__ flags) {
+    scal->time = time;
+    if (flags) *flags = 0u;
+}
+__global__ void k_report(const StepScalars* __restrict__ scal, const uint32_t* __restrict__ flags,
+                         HostReport* __restrict__ out) {
+    out->time = scal->time;
+    out->flags = *flags;
+}
+
+// rrsph_download into host arrays the device can address: one pass writing
+// the requested arrays (null: skipped) over the host link.
+template <int DIM>
+__global__ void k_download_direct(DevParams P, State S, double* __restrict__ r, double* __restrict__ v,
+                                  double* __restrict__ rho, double* __restrict__ p, int32_t* __restrict__ itype,
+                                  uint32_t stride, int vec) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const size_t b = (size_t)i * stride;
+    if (r) host_write3<DIM>(r, b, vec, S.rx[i], S.ry[i], DIM == 3 ? S.rz[i] : 0.0);
+    if (v) host_write3<DIM>(v, b, vec, S.vx[i], S.vy[i], DIM == 3 ? S.vz[i] : 0.0);
+    if (rho) rho[i] = S.rho[i];
+    if (p) p[i] = S.p[i];
+    if (itype) itype[i] = S.itype[i];
+}
+
 }  // namespace
+
+// 16-byte accesses for strided coordinate arrays where the layout allows.
+inline int vec_layout(int dim, uint32_t stride, const void* a, const void* b) {
+    const bool al = (reinterpret_cast<uintptr_t>(a) % 16 == 0) && (reinterpret_cast<uintptr_t>(b) % 16 == 0);
+    return al && ((dim == 2 && stride == 2) || (dim == 3 && stride == 4)) ? 1 : 0;
+}
+
+void launch_set_time(StepScalars* scal, double time, uint32_t* flags, cudaStream_t st) {
+    k_set_time<<<1, 1, 0, st>>>(scal, time, flags);
+}
+void launch_report(const StepScalars* scal, const uint32_t* flags, HostReport* out, cudaStream_t st) {
+    k_report<<<1, 1, 0, st>>>(scal, flags, out);
+}
+
+template <int DIM>
+void launch_upload_direct(const DevParams& P, const State& S, const Sorted& G, const double* r, const double* v,
+                          const double* rho, const double* p, const int32_t* itype, uint32_t stride,
+                          StepScalars* scal, double dt, uint32_t* flags, cudaStream_t st) {
+    k_upload_direct<DIM><<<blocks_for(P.n, 256), 256, 0, st>>>(P, S, G, r, v, rho, p, itype, stride,
+                                                               vec_layout(DIM, stride, r, v), scal, dt, flags);
+}
+template <int DIM>
+void launch_download_direct(const DevParams& P, const State& S, double* r, double* v, double* rho, double* p,
+                            int32_t* itype, uint32_t stride, cudaStream_t st) {
+    k_download_direct<DIM><<<blocks_for(P.n, 256), 256, 0, st>>>(P, S, r, v, rho, p, itype, stride,
+                                                                 vec_layout(DIM, stride, r, v));
+}
 
 template <int DIM>
 void launch_keys(const DevParams& P, const State& S, Sorted& G, StepScalars* scal, int predict, uint32_t* flags,
@@ -249,7 +385,12 @@ void launch_pack(const DevParams& P, State S, double* r, double* v, uint32_t str
     template void launch_neighbour_list<D>(const DevParams&, const Sorted&, uint32_t*, uint32_t*, uint32_t,    \
                                            uint32_t*, cudaStream_t);                                           \
     template void launch_unpack<D>(const DevParams&, State, const double*, const double*, uint32_t, cudaStream_t); \
-    template void launch_pack<D>(const DevParams&, State, double*, double*, uint32_t, cudaStream_t);
+    template void launch_pack<D>(const DevParams&, State, double*, double*, uint32_t, cudaStream_t);         \
+    template void launch_upload_direct<D>(const DevParams&, const State&, const Sorted&, const double*,        \
+                                          const double*, const double*, const double*, const int32_t*,         \
+                                          uint32_t, StepScalars*, double, uint32_t*, cudaStream_t);            \
+    template void launch_download_direct<D>(const DevParams&, const State&, double*, double*, double*, double*, \
+                                            int32_t*, uint32_t, cudaStream_t);
 RRSPH_INSTANTIATE(2)
 RRSPH_INSTANTIATE(3)
 #undef RRSPH_INSTANTIATE

@@ -506,7 +506,8 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
     }
     if (cudaMallocHost(&s->h_scal, sizeof(rrsph::StepScalars)) != cudaSuccess ||
         cudaMallocHost(&s->h_flags, sizeof(uint32_t)) != cudaSuccess ||
-        cudaMallocHost(&s->h_time, sizeof(double)) != cudaSuccess)
+        cudaHostAlloc(&s->h_report, sizeof(rrsph::HostReport), cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostGetDevicePointer((void**)&s->d_report, s->h_report, 0) != cudaSuccess)
         return fail(set_error(RRSPH_ERR_OUT_OF_MEMORY, "rrsph_create: pinned host allocation failed"));
     // empty cell table, zeroed state
     if (cudaMemsetAsync(G.cell_start, 0xFF, (size_t)s->P.max_cells * sizeof(uint32_t), s->stream) != cudaSuccess ||
@@ -536,7 +537,7 @@ extern "C" void rrsph_destroy(rrsph_solver* s) {
         if (a) cudaFree(a);
     if (s->h_scal) cudaFreeHost(s->h_scal);
     if (s->h_flags) cudaFreeHost(s->h_flags);
-    if (s->h_time) cudaFreeHost(s->h_time);
+    if (s->h_report) cudaFreeHost(s->h_report);
     if (s->h_vl) cudaFreeHost(s->h_vl);
     if (s->aux) cudaStreamDestroy(s->aux);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -549,6 +550,22 @@ extern "C" int rrsph_get_stream(rrsph_solver* s, void** stream) {
     return RRSPH_OK;
 }
 
+namespace {
+// The device address of a host array the device can reach (page-locked host
+// memory: cudaMallocHost / cudaHostAlloc / cudaHostRegister), else null.
+// Null in, null out.
+const void* device_view(const void* host) {
+    if (!host) return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+int finish_upload(rrsph_solver* s);
+}  // namespace
+
 extern "C" int rrsph_upload(rrsph_solver* s, const double* r, uint32_t stride, const double* v, const double* rho,
                             const double* pres, const int32_t* itype) {
     int rc = check_handle(s, "rrsph_upload");
@@ -556,9 +573,33 @@ extern "C" int rrsph_upload(rrsph_solver* s, const double* r, uint32_t stride, c
     if (!r || !v || !rho || !itype) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_upload: null array");
     if (stride < (uint32_t)s->dim) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_upload: stride < dim");
     const size_t n = s->P.n;
-    if ((rc = ensure_staging(s, 2 * n * stride)) != 0) return rc;
     auto& S = s->S;
     cudaStream_t st = s->stream;
+    // page-locked caller arrays: one kernel reads them over the host link
+    const double* dr = static_cast<const double*>(device_view(r));
+    const double* dv = static_cast<const double*>(device_view(v));
+    const double* drho = static_cast<const double*>(device_view(rho));
+    const double* dp = static_cast<const double*>(device_view(pres));
+    const int32_t* dit = static_cast<const int32_t*>(device_view(itype));
+    if (dr && dv && drho && dit && (dp || !pres)) {
+        if (s->verlet) set_verlet_copies(s, 0, 0);  // step 0 reads the copies its key pass writes
+        if (S.vl_rebuild) {  // before the key pass below, which may raise the flag again
+            rrsph::launch_verlet_upload_check(S.vl_rebuild, S.vl_gone, st);
+            s->launches++;
+        }
+        if (s->dim == 3)
+            rrsph::launch_upload_direct<3>(s->P, S, s->G, dr, dv, drho, dp, dit, stride, s->scal, s->params.dt,
+                                           s->flags, st);
+        else
+            rrsph::launch_upload_direct<2>(s->P, S, s->G, dr, dv, drho, dp, dit, stride, s->scal, s->params.dt,
+                                           s->flags, st);
+        s->launches++;
+        RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
+        s->step_index = 0;
+        s->keys_ready = true;  // the upload kernel ran the first step's key pass
+        return RRSPH_OK;
+    }
+    if ((rc = ensure_staging(s, 2 * n * stride)) != 0) return rc;
     RRSPH_CUDA_TRY(cudaMemcpyAsync(s->staging, r, n * stride * sizeof(double), cudaMemcpyHostToDevice, st));
     RRSPH_CUDA_TRY(cudaMemcpyAsync(s->staging + n * stride, v, n * stride * sizeof(double), cudaMemcpyHostToDevice, st));
     if (s->dim == 3) rrsph::launch_unpack<3>(s->P, S, s->staging, s->staging + n * stride, stride, st);
@@ -578,6 +619,15 @@ extern "C" int rrsph_upload(rrsph_solver* s, const double* r, uint32_t stride, c
         if (S.avz) RRSPH_CUDA_TRY(cudaMemsetAsync(S.avz, 0, n * sizeof(double), st));
     }
     RRSPH_CUDA_TRY(cudaMemsetAsync(S.drho, 0, n * sizeof(double), st));
+    return finish_upload(s);
+}
+
+namespace {
+// The rest of rrsph_upload after the state is on the device: the step
+// scalars, the neighbour-list check, and the wait for the caller's arrays.
+int finish_upload(rrsph_solver* s) {
+    auto& S = s->S;
+    cudaStream_t st = s->stream;
     rrsph::StepScalars init{};
     init.dt = s->params.dt;
     std::memcpy(s->h_scal, &init, sizeof(init));
@@ -591,6 +641,7 @@ extern "C" int rrsph_upload(rrsph_solver* s, const double* r, uint32_t stride, c
     s->keys_ready = false;
     return RRSPH_OK;
 }
+}  // namespace
 
 extern "C" int rrsph_download(rrsph_solver* s, double* r, uint32_t stride, double* v, double* rho, double* pres,
                               int32_t* itype) {
@@ -599,6 +650,19 @@ extern "C" int rrsph_download(rrsph_solver* s, double* r, uint32_t stride, doubl
     if ((r || v) && stride < (uint32_t)s->dim) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_download: stride < dim");
     const size_t n = s->P.n;
     cudaStream_t st = s->stream;
+    // page-locked caller arrays: one kernel writes them over the host link
+    double* dr = const_cast<double*>(static_cast<const double*>(device_view(r)));
+    double* dv = const_cast<double*>(static_cast<const double*>(device_view(v)));
+    double* drho = const_cast<double*>(static_cast<const double*>(device_view(rho)));
+    double* dp = const_cast<double*>(static_cast<const double*>(device_view(pres)));
+    int32_t* dit = const_cast<int32_t*>(static_cast<const int32_t*>(device_view(itype)));
+    if ((dr || !r) && (dv || !v) && (drho || !rho) && (dp || !pres) && (dit || !itype)) {
+        if (s->dim == 3) rrsph::launch_download_direct<3>(s->P, s->S, dr, dv, drho, dp, dit, stride, st);
+        else rrsph::launch_download_direct<2>(s->P, s->S, dr, dv, drho, dp, dit, stride, st);
+        s->launches++;
+        RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
+        return RRSPH_OK;
+    }
     if (r || v) {
         if ((rc = ensure_staging(s, 2 * n * stride)) != 0) return rc;
         if (s->dim == 3) rrsph::launch_pack<3>(s->P, s->S, r ? s->staging : nullptr, v ? s->staging + n * stride : nullptr, stride, st);
@@ -675,11 +739,10 @@ int enqueue_steps(rrsph_solver* s, uint64_t nsteps) {
 extern "C" int rrsph_set_time(rrsph_solver* s, double time) {
     int rc = check_handle(s, "rrsph_set_time");
     if (rc) return rc;
-    // the pinned staging word may still be read by an earlier copy
-    RRSPH_CUDA_TRY(cudaStreamSynchronize(s->stream));
-    *s->h_time = time;
     const int par = (int)(s->step_index & 1);
-    RRSPH_CUDA_TRY(cudaMemcpyAsync(&s->scal[par].time, s->h_time, sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    rrsph::launch_set_time(&s->scal[par], time, nullptr, s->stream);
+    RRSPH_CUDA_TRY(cudaGetLastError());
+    s->launches++;
     return RRSPH_OK;
 }
 
@@ -694,20 +757,21 @@ extern "C" int rrsph_sync(rrsph_solver* s, double* time_out) {
     if (rc) return rc;
     cudaStream_t st = s->stream;
     const int parn = (int)(s->step_index & 1);
-    RRSPH_CUDA_TRY(cudaMemcpyAsync(s->h_scal, &s->scal[parn], sizeof(rrsph::StepScalars), cudaMemcpyDeviceToHost, st));
-    RRSPH_CUDA_TRY(cudaMemcpyAsync(s->h_flags, s->flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    rrsph::launch_report(&s->scal[parn], s->flags, s->d_report, st);
+    s->launches++;
     RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
     RRSPH_CUDA_TRY(cudaGetLastError());
-    if (time_out) *time_out = s->h_scal->time;
-    return flags_to_status(s, *s->h_flags);
+    if (time_out) *time_out = s->h_report->time;
+    return flags_to_status(s, s->h_report->flags);
 }
 
 extern "C" int rrsph_step(rrsph_solver* s, uint64_t nsteps, double* time_io) {
     int rc = check_handle(s, "rrsph_step");
     if (rc) return rc;
     if (!time_io) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_step: null time");
-    if ((rc = rrsph_set_time(s, *time_io)) != 0) return rc;
-    RRSPH_CUDA_TRY(cudaMemsetAsync(s->flags, 0, sizeof(uint32_t), s->stream));
+    rrsph::launch_set_time(&s->scal[s->step_index & 1], *time_io, s->flags, s->stream);  // time, flags cleared
+    RRSPH_CUDA_TRY(cudaGetLastError());
+    s->launches++;
     if ((rc = enqueue_steps(s, nsteps)) != 0) return rc;
     return rrsph_sync(s, time_io);
 }

@@ -32,7 +32,8 @@ struct rrsph_solver {
     uint32_t* flags = nullptr;
     rrsph::StepScalars* h_scal = nullptr;  // pinned
     uint32_t* h_flags = nullptr;           // pinned
-    double* h_time = nullptr;              // pinned
+    rrsph::HostReport* h_report = nullptr;  // mapped pinned mailbox of k_report
+    rrsph::HostReport* d_report = nullptr;  // its device address
     double* staging = nullptr;
     size_t staging_words = 0;
     std::vector<void*> allocations;

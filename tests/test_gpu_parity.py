@@ -574,3 +574,55 @@ def test_neighbour_reuse_across_uploads(gpu_available):
     for k in ("r", "v", "rho", "p"):
         assert np.array_equal(again[k], ref5[k]), k
         assert np.array_equal(back[k], ref1[k]), k
+
+
+def test_pinned_host_arrays_upload_and_download_directly(gpu_available):
+    """Page-locked caller arrays go through one kernel each way (read and
+    written over the host link); the state equals that of pageable arrays,
+    which go through copies, bit for bit, in 2D and 3D (stride 4 as for the
+    padded rr_float3)."""
+    import torch
+
+    from sph2d_gb300 import Solver, cases, capi
+    import ctypes as C
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=getattr(torch, str(a.dtype)), pin_memory=True)
+        t.numpy()[...] = a
+        return t
+
+    L = capi.lib()
+    dp = lambda x: x.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    ip = lambda x: x.ctypes.data_as(C.POINTER(C.c_int32))  # noqa: E731
+    for case, stride in ((_dam(nx=40, ny=20), 2), (cases.dam_break_3d(dx=0.02, block=(0.2, 0.3, 0.2)), 4)):
+        p = case.params()
+        n, dim = case.ntotal, case.r.shape[1]
+        r = np.zeros((n, stride))
+        v = np.zeros((n, stride))
+        r[:, :dim], v[:, :dim] = case.r, case.v
+        pres = np.full(n, 3.0)
+        out = []
+        for pin in (False, True):
+            keep = []
+            arrs = [r, v, case.rho, pres, case.itype]
+            if pin:
+                keep = [pinned(a) for a in arrs]
+                arrs = [t.numpy() for t in keep]
+            hr, hv, hrho, hp, hit = arrs
+            res = {k: np.zeros_like(a) for k, a in (("r", r), ("v", v), ("rho", case.rho), ("p", pres),
+                                                      ("itype", case.itype))}
+            if pin:
+                keep += [pinned(a) for a in res.values()]
+                res = dict(zip(res.keys(), [t.numpy() for t in keep[5:]]))
+            with Solver(p, "mixed") as s:
+                capi.check(L.rrsph_upload(s.handle, dp(hr), stride, dp(hv), dp(hrho), dp(hp), ip(hit)))
+                t = C.c_double(0.0)
+                capi.check(L.rrsph_step(s.handle, 3, C.byref(t)))
+                capi.check(L.rrsph_download(s.handle, dp(res["r"]), stride, dp(res["v"]), dp(res["rho"]),
+                                            dp(res["p"]), ip(res["itype"])))
+            out.append({k: np.array(a, copy=True) for k, a in res.items()})
+        for k in ("r", "v", "rho", "p", "itype"):
+            a, b = out[0][k], out[1][k]
+            if k in ("r", "v"):
+                a, b = a[:, :dim], b[:, :dim]
+            assert np.array_equal(a, b), (dim, k)
