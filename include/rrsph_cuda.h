@@ -360,8 +360,8 @@ int rrsph_set_gather_threads(rrsph_solver* s, uint32_t density_threads, uint32_t
  * state back. threads_out[2] (may be NULL) receives {density, forces}. */
 int rrsph_autotune(rrsph_solver* s, uint32_t steps, uint32_t* threads_out);
 
-/* Neighbour reuse of the 2D FP32-mixed step with summation density (on by
- * default there): each particle's candidate list holds the particles within
+/* Neighbour reuse of the FP32-mixed step, 2D or 3D, summation or continuity
+ * density (on by default there): each particle's candidate list holds the particles within
  * (cell_scale_k + skin_over_h) * hsml of it at the last grid build, and the
  * grid and lists are rebuilt only when a particle has moved more than half the
  * skin since then, so every pair within the cutoff stays in the lists. Each

@@ -32,8 +32,8 @@ ORACLE_LIB = ORACLE_DIR / "liboracle.so"
 REF_BIN = ORACLE_DIR / "_ref" / "rrsph_ref"
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CU_SOURCES = ["sort.cu", "kernels_common.cu", "kernels_fp64.cu", "kernels_mixed.cu", "solver.cu", "sort_noalloc.cu",
-              "run_loop.cu", "adjoint.cu"]
+CU_SOURCES = ["sort.cu", "kernels_common.cu", "kernels_fp64.cu", "kernels_mixed.cu", "kernels_reuse.cu", "solver.cu",
+              "sort_noalloc.cu", "run_loop.cu", "adjoint.cu"]
 CPP_SOURCES = ["params.cpp", "layers.cpp"]
 
 

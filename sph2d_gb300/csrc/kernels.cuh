@@ -26,11 +26,12 @@ struct State {
     float4* coff4;             // 3D: the same (x, y, z)
     float2* vpf2;              // 2D: v_predict in float
     float4* vpf4;              // 3D: the same (x, y, z)
-    // 2D mixed step with neighbour reuse (null otherwise), id order:
-    uint32_t* cxy;             // cell coordinates of the current position, x | y << 16
+    // mixed step with neighbour reuse (null otherwise), id order:
+    uint32_t* cxy;             // cell coordinates of the current position, x | y << 16 (3D: x | y << 10 | z << 20)
     uint32_t* bcxy;            // cell coordinates at the last list build
     uint32_t* slot;            // cell-order index at the last list build
-    float2* boff;              // offset from that cell's edge at the last list build
+    float2* boff;              // 2D: offset from that cell's edges at the last list build
+    float4* boff4;             // 3D: the same (x, y, z)
     uint32_t* vl_rebuild;      // non-zero: the next step rebuilds the grid and the lists
     uint32_t* vl_gone;         // the last build: bit 0 left out non-existent particles, bit 1 overflowed a list
 };
@@ -55,17 +56,20 @@ struct Sorted {
     float4* V4;    // velocity the forces use + density the forces use
     float4* VD4;   // v + (rho - rho0) for density_con
     float2* PR;    // pressure p and p / rho^2 (rho = the density the forces use)
-    // 2D mixed step with neighbour reuse: the P4 / V4 of the next step, which the
-    // key pass writes at each particle's build slot (the two buffers alternate)
+    // mixed step with neighbour reuse: the P4 / V4 (/ VD4 with continuity
+    // density) of the next step, which the key pass writes at each particle's
+    // build slot (the two buffers alternate)
     float4* P4n;
     float4* V4n;
+    float4* VD4n;
     // 2D mixed step: neighbour masks written by the density pass for the force
     // pass, SoA [10][n]: word c < 9 = bit b set if particle cell_start + b of
     // stencil cell c is a neighbour; word 9 = stencil cells with more than 32
     // particles (searched again by the force pass). Null where unused.
     uint32_t* nbmask;
-    // 2D mixed step with neighbour reuse: up to kVerletCap candidates per
-    // particle, sorted index | cell code << 27 with code = (dx + 2) * 5 + (dy + 2)
+    // mixed step with neighbour reuse: up to kVerletCap2 (2D) / kVerletCap3 (3D)
+    // candidates per particle, sorted index | cell code << 27 (3D: << 25) with
+    // code = (dx + 2) * 5 + (dy + 2) (3D: ((dx + 2) * 5 + (dy + 2)) * 5 + (dz + 2))
     // for the candidate's cell offset, stored in slabs of four: entries 4g..4g+3
     // of particle k are the uint4 at (uint4*)list + g * n + k (the lanes of a
     // warp read neighbouring uint4s), the last group padded with kVlNone;
@@ -112,18 +116,21 @@ void launch_whole_step(const DevParams& P, const State& S, const Sorted& G, Step
 
 // Neighbour reuse (2D mixed step with summation density): the candidate lists
 // are built with the cutoff widened by a skin and reused while no particle has
-// moved more than half the skin since the build (kernels_mixed.cu).
+// moved more than half the skin since the build (kernels_reuse.cu).
 void launch_verlet_decide(cudaGraphConditionalHandle h, const uint32_t* rebuild, cudaStream_t st);
 void launch_verlet_reset(uint32_t* rebuild, uint32_t* gone, unsigned long long* builds, cudaStream_t st);
 // After an upload: the lists stay valid unless the last build left out a
 // non-existent particle (which may exist now); moves are checked by the key pass.
 void launch_verlet_upload_check(uint32_t* rebuild, const uint32_t* gone, cudaStream_t st);
+template <int DIM>
 void launch_verlet_build(const DevParams& P, const State& S, const Sorted& G, cudaStream_t st);
+template <int DIM>
 void launch_density_verlet(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
                            cudaStream_t st, int threads);
 // whole != 0: the whole step of each particle (launch_whole_step with next keys)
 // runs in the force gather's thread; needs dt without the step's reduction and
-// at most kVerletCap + 1 neighbours per particle (max_nb).
+// at most verlet_cap(dim) + 1 neighbours per particle (max_nb).
+template <int DIM>
 void launch_forces_verlet(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal,
                           StepScalars* scal_next, uint32_t* flags, cudaStream_t st, int threads, int whole);
 
@@ -154,7 +161,11 @@ template <int DIM>
 void launch_download_direct(const DevParams& P, const State& S, double* r, double* v, double* rho, double* p,
                             int32_t* itype, uint32_t stride, cudaStream_t st);
 
-constexpr int kVerletCap = 64;          // candidate-list entries per particle
+constexpr int kVerletCap2 = 64;         // candidate-list entries per particle, 2D
+constexpr int kVerletCap3 = 256;        // and 3D
+inline int verlet_cap(int dim) { return dim == 3 ? kVerletCap3 : kVerletCap2; }
+// particles a list entry can index (the cell code takes the top bits)
+inline uint64_t verlet_max_particles(int dim) { return dim == 3 ? (1ull << 25) : (1ull << 27); }
 constexpr uint32_t kListOver = 0xFFFFFFFFu;
 constexpr uint32_t kVlNone = 0xFFFFFFFFu;  // padding of a list row (never an entry)
 constexpr int kGatherThreads = 128;     // default block size of the pair gathers

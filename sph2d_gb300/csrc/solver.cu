@@ -248,6 +248,10 @@ void set_verlet_copies(rrsph_solver* s, int read, int write) {
     s->G.V4 = s->v4buf[read];
     s->G.P4n = s->p4buf[write];
     s->G.V4n = s->v4buf[write];
+    if (s->G.VD4n) {
+        s->G.VD4 = s->vd4buf[read];
+        s->G.VD4n = s->vd4buf[write];
+    }
 }
 
 void enqueue_verlet_rebuild(rrsph_solver* s, cudaStream_t st) {
@@ -256,9 +260,15 @@ void enqueue_verlet_rebuild(rrsph_solver* s, cudaStream_t st) {
                                  s->G.sort_scratch, s->P.n, s->sort_bits, st, &s->launches);
     s->G.key = s->G.keys_a;
     s->G.id = s->G.ids_a;
-    rrsph::GatherSrc fsrc{s->S.vpx, s->S.vpy, s->S.vpz, s->S.rho, nullptr, 1};
-    rrsph::launch_reorder<2>(s->P, s->S, s->G, fsrc, 1, st);
-    rrsph::launch_verlet_build(s->P, s->S, s->G, st);
+    const bool cont = s->P.density_treatment != 0;
+    rrsph::GatherSrc fsrc{s->S.vpx, s->S.vpy, s->S.vpz, cont ? s->S.rho_pred : s->S.rho, nullptr, 1};
+    if (s->dim == 3) {
+        rrsph::launch_reorder<3>(s->P, s->S, s->G, fsrc, 1, st);
+        rrsph::launch_verlet_build<3>(s->P, s->S, s->G, st);
+    } else {
+        rrsph::launch_reorder<2>(s->P, s->S, s->G, fsrc, 1, st);
+        rrsph::launch_verlet_build<2>(s->P, s->S, s->G, st);
+    }
     s->launches += 3;
 }
 
@@ -274,7 +284,8 @@ int enqueue_step_verlet(rrsph_solver* s, int par, cudaEvent_t* events, bool with
     if (events) cudaEventRecord(events[0], st);
     if (with_keys) set_verlet_copies(s, par, par);  // this step's copies from its own key pass
     if (with_keys) {
-        rrsph::launch_keys<2>(s->P, s->S, s->G, cur, 1, s->flags, st);
+        if (s->dim == 3) rrsph::launch_keys<3>(s->P, s->S, s->G, cur, 1, s->flags, st);
+        else rrsph::launch_keys<2>(s->P, s->S, s->G, cur, 1, s->flags, st);
         s->launches++;
     }
     set_verlet_copies(s, par, par ^ 1);
@@ -314,14 +325,20 @@ int enqueue_step_verlet(rrsph_solver* s, int par, cudaEvent_t* events, bool with
         cudaEventRecord(events[2], st);
         cudaEventRecord(events[3], st);
     }
-    rrsph::launch_density_verlet(s->P, s->S, s->G, cur, s->flags, st, s->gather_threads[0]);
+    const bool d3 = s->dim == 3;
+    if (d3) rrsph::launch_density_verlet<3>(s->P, s->S, s->G, cur, s->flags, st, s->gather_threads[0]);
+    else rrsph::launch_density_verlet<2>(s->P, s->S, s->G, cur, s->flags, st, s->gather_threads[0]);
     if (events) cudaEventRecord(events[4], st);
     // the whole step runs inside the force gather unless dt waits for the step's
     // maxima or a particle may have more neighbours than a list holds
-    const bool fuse = !(s->P.dt_method == 2 && s->P.dt_reduce) && s->P.max_nb <= rrsph::kVerletCap + 1;
-    rrsph::launch_forces_verlet(s->P, s->S, s->G, cur, nxt, s->flags, st, s->gather_threads[1], fuse ? 1 : 0);
+    const bool fuse = !(s->P.dt_method == 2 && s->P.dt_reduce) && s->P.max_nb <= rrsph::verlet_cap(s->dim) + 1;
+    if (d3) rrsph::launch_forces_verlet<3>(s->P, s->S, s->G, cur, nxt, s->flags, st, s->gather_threads[1], fuse ? 1 : 0);
+    else rrsph::launch_forces_verlet<2>(s->P, s->S, s->G, cur, nxt, s->flags, st, s->gather_threads[1], fuse ? 1 : 0);
     if (events) cudaEventRecord(events[5], st);
-    if (!fuse) rrsph::launch_whole_step<2>(s->P, s->S, s->G, cur, nxt, s->flags, 1, st);
+    if (!fuse) {
+        if (d3) rrsph::launch_whole_step<3>(s->P, s->S, s->G, cur, nxt, s->flags, 1, st);
+        else rrsph::launch_whole_step<2>(s->P, s->S, s->G, cur, nxt, s->flags, 1, st);
+    }
     if (events) cudaEventRecord(events[6], st);
     s->launches += fuse ? 2 : 3;
     return RRSPH_OK;
@@ -450,7 +467,9 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
     if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess)
         return fail(set_error(RRSPH_ERR_CUDA, "rrsph_create: cudaStreamCreate failed"));
 #define A(ptr, count) \
-    if ((rc = dev_alloc(s, &(ptr), (count))) != 0) return fail(rc)
+    do {                                                 \
+        if ((rc = dev_alloc(s, &(ptr), (count))) != 0) return fail(rc); \
+    } while (0)
     A(S.rx, n); A(S.ry, n); A(S.vx, n); A(S.vy, n); A(S.ax, n); A(S.ay, n); A(S.vpx, n); A(S.vpy, n);
     if (d3) { A(S.rz, n); A(S.vz, n); A(S.az, n); A(S.vpz, n); }
     if (p->average_velocity) { A(S.avx, n); A(S.avy, n); if (d3) A(S.avz, n); }
@@ -467,20 +486,31 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
         if (cont) { A(G.vdx, n); A(G.vdy, n); if (d3) A(G.vdz, n); A(G.rhod, n); }
     } else {
         if (d3) { A(S.coff4, n); A(S.vpf4, n); } else { A(S.coff2, n); A(S.vpf2, n); }
-        if (!d3 && !cont) {  // neighbour reuse
-            A(S.cxy, n); A(S.bcxy, n); A(S.slot, n); A(S.boff, n); A(S.vl_rebuild, 2); A(s->vl_builds, 1);
+        if (n < rrsph::verlet_max_particles(s->dim)) {  // neighbour reuse
+            const size_t cap = (size_t)rrsph::verlet_cap(s->dim);
+            A(S.cxy, n); A(S.bcxy, n); A(S.slot, n); A(S.vl_rebuild, 2); A(s->vl_builds, 1);
+            if (d3) {
+                A(S.boff4, n);
+            } else {
+                A(S.boff, n);
+            }
             S.vl_gone = S.vl_rebuild + 1;
-            A(G.vlist, (size_t)rrsph::kVerletCap * n); A(G.vcount, n); A(G.nlist, (size_t)rrsph::kVerletCap * n); A(G.ncount, n);
+            A(G.vlist, cap * n); A(G.vcount, n); A(G.nlist, cap * n); A(G.ncount, n);
             A(G.keys_b, n); A(G.ids_b, n);
         }
         A(G.P4, n); A(G.V4, n); A(G.PR, n);
+        if (cont) A(G.VD4, n);
         s->p4buf[0] = s->p4buf[1] = G.P4;
         s->v4buf[0] = s->v4buf[1] = G.V4;
-        if (G.vlist) { A(s->p4buf[1], n); A(s->v4buf[1], n); }
+        s->vd4buf[0] = s->vd4buf[1] = G.VD4;
+        if (G.vlist) {
+            A(s->p4buf[1], n); A(s->v4buf[1], n);
+            if (cont) A(s->vd4buf[1], n);
+        }
         G.P4n = s->p4buf[1];
         G.V4n = s->v4buf[1];
+        G.VD4n = cont ? s->vd4buf[1] : nullptr;
         if (!d3) A(G.nbmask, 10 * n);
-        if (cont) A(G.VD4, n);
     }
     A(s->scal, 2);
     A(s->flags, 1);
@@ -490,17 +520,27 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
             cudaMallocHost(&s->h_vl, sizeof(uint32_t)) != cudaSuccess)
             return fail(set_error(RRSPH_ERR_CUDA, "rrsph_create: neighbour-reuse stream"));
         // no lists yet: empty lists, masks and grid until the first build (which the flag forces)
-        if (cudaMemsetAsync(S.vl_rebuild, 0xFF, sizeof(uint32_t), s->stream) != cudaSuccess ||
-            cudaMemsetAsync(S.vl_gone, 0, sizeof(uint32_t), s->stream) != cudaSuccess ||
-            cudaMemsetAsync(s->vl_builds, 0, sizeof(unsigned long long), s->stream) != cudaSuccess ||
-            cudaMemsetAsync(G.vcount, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
-            cudaMemsetAsync(G.ncount, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
-            cudaMemsetAsync(S.bcxy, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
-            cudaMemsetAsync(S.slot, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
-            cudaMemsetAsync(S.boff, 0, n * sizeof(float2), s->stream) != cudaSuccess ||
-            cudaMemsetAsync(G.keys_a, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
-            cudaMemsetAsync(G.ids_a, 0, n * sizeof(uint32_t), s->stream) != cudaSuccess)
-            return fail(set_error(RRSPH_ERR_CUDA, "rrsph_create: memset failed"));
+        const struct {
+            void* ptr;
+            int value;
+            size_t bytes;
+            const char* name;
+        } zero[] = {{S.vl_rebuild, 0xFF, sizeof(uint32_t), "rebuild flag"},
+                    {S.vl_gone, 0, sizeof(uint32_t), "build flags"},
+                    {s->vl_builds, 0, sizeof(unsigned long long), "build count"},
+                    {G.vcount, 0, n * sizeof(uint32_t), "candidate counts"},
+                    {G.ncount, 0, n * sizeof(uint32_t), "neighbour counts"},
+                    {S.bcxy, 0, n * sizeof(uint32_t), "build cells"},
+                    {S.slot, 0, n * sizeof(uint32_t), "build slots"},
+                    {d3 ? (void*)S.boff4 : (void*)S.boff, 0, n * (d3 ? sizeof(float4) : sizeof(float2)), "build offsets"},
+                    {G.keys_a, 0, n * sizeof(uint32_t), "grid keys"},
+                    {G.ids_a, 0, n * sizeof(uint32_t), "grid ids"}};
+        for (const auto& z : zero) {
+            const cudaError_t e = cudaMemsetAsync(z.ptr, z.value, z.bytes, s->stream);
+            if (e != cudaSuccess)
+                return fail(set_error(RRSPH_ERR_CUDA, std::string("rrsph_create: memset of the ") + z.name +
+                                                          " failed: " + cudaGetErrorString(e)));
+        }
         s->verlet = true;
         set_verlet_params(s);
     }
@@ -514,7 +554,8 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
         cudaMemsetAsync(S.key_of, 0xFF, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
         cudaMemsetAsync(s->scal, 0, 2 * sizeof(rrsph::StepScalars), s->stream) != cudaSuccess ||
         cudaMemsetAsync(s->flags, 0, sizeof(uint32_t), s->stream) != cudaSuccess)
-        return fail(set_error(RRSPH_ERR_CUDA, "rrsph_create: memset failed"));
+        return fail(set_error(RRSPH_ERR_CUDA, std::string("rrsph_create: memset failed: ") +
+                                                  cudaGetErrorString(cudaGetLastError())));
     for (int i = 0; i <= kPhases; i++) {
         if (cudaEventCreate(&s->ev[i]) != cudaSuccess) return fail(set_error(RRSPH_ERR_CUDA, "rrsph_create: event"));
     }
@@ -987,7 +1028,8 @@ extern "C" int rrsph_set_neighbour_reuse(rrsph_solver* s, int enable, double ski
     int rc = check_handle(s, "rrsph_set_neighbour_reuse");
     if (rc) return rc;
     if (enable && !s->S.vl_rebuild)
-        return set_error(RRSPH_ERR_UNSUPPORTED, "neighbour reuse needs a 2D FP32-mixed solver with summation density");
+        return set_error(RRSPH_ERR_UNSUPPORTED, "neighbour reuse needs an FP32-mixed solver (at most 2^27 particles "
+                                                "in 2D, 2^25 in 3D)");
     if (enable && !(skin_over_h > 0 && skin_over_h <= 1))
         return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_set_neighbour_reuse: skin must be in (0, 1] hsml");
     drop_graphs(s);

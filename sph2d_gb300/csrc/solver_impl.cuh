@@ -58,10 +58,11 @@ struct rrsph_solver {
     uint32_t* h_vl = nullptr;                  // pinned: the rebuild flag, read with direct launches
     cudaGraph_t vl_body = nullptr;  // rebuild body of the graph being captured
     bool vl_pending = false;
-    // neighbour reuse: the two P4 / V4 buffers (a step reads [parity], its key
+    // neighbour reuse: the two P4 / V4 (/ VD4) buffers (a step reads [parity], its key
     // pass writes the next step's into [parity ^ 1])
     float4* p4buf[2] = {nullptr, nullptr};
     float4* v4buf[2] = {nullptr, nullptr};
+    float4* vd4buf[2] = {nullptr, nullptr};  // continuity density
     unsigned long long vl_extra_launches = 0;  // launches a rebuild adds to a reuse step
 };
 

@@ -38,6 +38,39 @@ __device__ __forceinline__ bool in_geometry(const DevParams& P, double x, double
 enum : int { kVarCont = 1, kVarRare = 2, kVarMixed = 4 };  // continuity, XSPH or dynamic dt, FP32-mixed
 // M: 0 = FP64 step, 1 = FP32-mixed step, 2 = decided at run time from the state's buffers.
 
+// Neighbour reuse, in the key pass of particle i: the next step's cell-order
+// copies at the particle's slot of the last build, with (px, py, pz) its offset
+// from the edge of its build cell (a step that rebuilds overwrites them in its
+// new order). With continuity density V4.w is rho_predict and VD4 = (v,
+// rho - rho0), as the reorder writes them.
+template <int DIM>
+__device__ __forceinline__ void reuse_copies(const DevParams& P, const State& S, const Sorted& G, uint32_t i,
+                                             float px, float py, float pz) {
+    const uint32_t k = S.slot[i];
+    G.P4n[k] = make_float4(px, py, pz, __int_as_float(S.itype[i]));
+    float4 v;
+    if (DIM == 3) {
+        v = S.vpf4[i];
+        v.w = 0.0f;
+    } else {
+        const float2 v2 = S.vpf2[i];
+        v = make_float4(v2.x, v2.y, 0.0f, 0.0f);  // .zw (summation): the density pass writes them
+    }
+    if (G.VD4n) {
+        v.w = d2f(S.rho_pred[i]);
+        G.VD4n[k] = make_float4(d2f(S.vx[i]), d2f(S.vy[i]), DIM == 3 ? d2f(S.vz[i]) : 0.0f,
+                                d2f(S.rho[i] - P.rho0));
+    }
+    G.V4n[k] = v;
+}
+// A particle that moved more than half the skin since the build asks for a
+// rebuild (one atomic per warp).
+__device__ __forceinline__ void reuse_check(const State& S, bool moved) {
+    const unsigned am = __activemask();
+    const unsigned who = __ballot_sync(am, moved);
+    if (who && (threadIdx.x & 31) == (unsigned)(__ffs(am) - 1)) atomicOr(S.vl_rebuild, 1u);
+}
+
 template <int DIM, int M>
 __device__ __forceinline__ void key_pass(const DevParams& P, const State& S, const Sorted& G, uint32_t i, double x,
                                          double y, double z, uint32_t* __restrict__ flags) {
@@ -81,23 +114,28 @@ __device__ __forceinline__ void key_pass(const DevParams& P, const State& S, con
             // offset from the edge of the cell the particle had at the build
             const float px = ox + (float)((int)cx - (int)(b & 0xFFFFu)) * P.mf.cell;
             const float py = oy + (float)((int)cy - (int)(b >> 16)) * P.mf.cell;
-            // the next step's cell-order copies, at the particle's slot of the build
-            // (a step that rebuilds overwrites them in its new order)
-            const uint32_t k = S.slot[i];
-            G.P4n[k] = make_float4(px, py, 0.0f, __int_as_float(S.itype[i]));
-            const float2 v = S.vpf2[i];
-            G.V4n[k] = make_float4(v.x, v.y, 0.0f, 0.0f);  // .zw: the density pass writes them
+            reuse_copies<DIM>(P, S, G, i, px, py, 0.0f);
             const float dx = px - bo.x, dy = py - bo.y;
-            const bool moved = !(dx * dx + dy * dy <= P.vl_half_skin2);
-            const unsigned am = __activemask();
-            const unsigned who = __ballot_sync(am, moved);
-            if (who && (threadIdx.x & 31) == (unsigned)(__ffs(am) - 1)) atomicOr(S.vl_rebuild, 1u);
+            reuse_check(S, !(dx * dx + dy * dy <= P.vl_half_skin2));
         }
     } else if (DIM == 3 && (M == 1 || S.coff4)) {
         const float ox = sx.off + (float)(uint32_t)(sx.c & ~0x3FFull) * P.mf.cell;
         const float oy = sy.off + (float)(uint32_t)(sy.c & ~0x3FFull) * P.mf.cell;
         const float oz = sz.off + (float)(uint32_t)(sz.c & ~0x3FFull) * P.mf.cell;
         S.coff4[i] = make_float4(ox, oy, oz, 0.0f);
+        if (S.cxy) {
+            const uint32_t cx = (uint32_t)(sx.c & 0x3FFu), cy = (uint32_t)(sy.c & 0x3FFu),
+                           cz = (uint32_t)(sz.c & 0x3FFu);
+            S.cxy[i] = cx | (cy << 10) | (cz << 20);
+            const uint32_t b = S.bcxy[i];
+            const float4 bo = S.boff4[i];
+            const float px = ox + (float)((int)cx - (int)(b & 0x3FFu)) * P.mf.cell;
+            const float py = oy + (float)((int)cy - (int)((b >> 10) & 0x3FFu)) * P.mf.cell;
+            const float pz = oz + (float)((int)cz - (int)(b >> 20)) * P.mf.cell;
+            reuse_copies<DIM>(P, S, G, i, px, py, pz);
+            const float dx = px - bo.x, dy = py - bo.y, dz = pz - bo.z;
+            reuse_check(S, !(dx * dx + dy * dy + dz * dz <= P.vl_half_skin2));
+        }
     }
 }
 
