@@ -53,6 +53,12 @@ L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
 # threads load (L1/L2), not algorithmic bytes.
 FORCES_REUSE_BYTES_PER_PARTICLE = (52 + 16) + (32 + 4 + 4 + 4 + 8 + 4) + (32 + 8 + 8 + 4 + 4 + 8 + 32 + 4)
 FORCES_REUSE_BYTES_PER_PAIR = 4
+# Pair arithmetic of the FP32 pipe per directed pair: 16 flops for the density
+# (distance, kernel, sum) and 52 for the forces (form-2 pressure term,
+# artificial viscosity, Lennard-Jones amortised); the nominal FP32 (non-tensor)
+# peak of the part is 152 SMs x 128 lanes x 2 flops x 2.07 GHz.
+FLOPS_PER_PAIR = 16 + 52
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 FORCES_FP64_BYTES_PER_PARTICLE_2D = 4 + 4 + 16 + 4 + 16 + 8 + 8 + 16
 
 
@@ -320,6 +326,14 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
             "traffic": traffic,
             "algorithmic_bytes_per_launch": bytes_launch,
             "avg_launch_ms": f_ms,
+        },
+        "fp32_pipe": {
+            "flops_per_pair": FLOPS_PER_PAIR,
+            "achieved_tflops": value * FLOPS_PER_PAIR / 1e12,
+            "peak_tflops": FP32_PEAK_TFLOPS,
+            "frac": value * FLOPS_PER_PAIR / 1e12 / FP32_PEAK_TFLOPS,
+            "peak_source": "nominal",
+            "note": "whole mixed step; the gathers are latency-bound on L1/L2 neighbour loads (ncu in profiles/)",
         },
         "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": e2e_steps, "path": "rrsph_upload + rrsph_step(1) + rrsph_download, pinned host buffers"},
