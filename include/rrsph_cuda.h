@@ -242,6 +242,25 @@ int rrsph_run(rrsph_solver* s, const char* experiment_dir, double* time_io,
               uint64_t max_steps, uint64_t* steps_done);
 /* Sticky RRSPH_FLAG_* bits raised by device checks since the last clear. */
 int rrsph_status(rrsph_solver* s, uint32_t* flags, int clear);
+
+/* Global checks of the current state, summed in double on the device in a
+ * fixed order (the same bits every call on the same state). No counterpart in
+ * the reference: the mass and energy checks that stay in double beside the
+ * FP32-mixed step. Fluid particles (itype > 0): mass, kinetic energy
+ * m|v|^2/2, potential energy m g y, the Tait EOS's internal energy m e(rho)
+ * (e = the integral of p/rho^2 from rho0) and momentum; boundary particles
+ * (itype < 0): mass. Non-existent particles count nowhere. */
+typedef struct rrsph_diagnostics {
+    double mass;           /* fluid */
+    double kinetic;        /* fluid */
+    double potential;      /* fluid, g along -y */
+    double internal;       /* fluid */
+    double momentum[3];    /* fluid; [2] = 0 in 2D */
+    double mass_boundary;  /* boundary particles */
+    uint64_t fluid;        /* fluid particles */
+    uint64_t boundary;     /* boundary particles */
+} rrsph_diagnostics;
+int rrsph_diagnostics_get(rrsph_solver* s, rrsph_diagnostics* out);
 /* Directed neighbour pairs (the entries find_neighbours would list) of the
  * last completed step, and summed over the steps since rrsph_upload. */
 int rrsph_pair_count(rrsph_solver* s, uint64_t* last_step, uint64_t* total);

@@ -117,6 +117,21 @@ class RrsphAdjointConfig(C.Structure):
     ]
 
 
+class RrsphDiagnostics(C.Structure):
+    """Mirror of rrsph_diagnostics."""
+
+    _fields_ = [
+        ("mass", C.c_double),
+        ("kinetic", C.c_double),
+        ("potential", C.c_double),
+        ("internal", C.c_double),
+        ("momentum", C.c_double * 3),
+        ("mass_boundary", C.c_double),
+        ("fluid", C.c_uint64),
+        ("boundary", C.c_uint64),
+    ]
+
+
 class RrsphWaveMaker(C.Structure):
     """Mirror of rrsph_wave_maker."""
 
@@ -162,6 +177,7 @@ _SIGS = {
     "rrsph_sync": (C.c_int, [C.c_void_p, _dp]),
     "rrsph_run": (C.c_int, [C.c_void_p, C.c_char_p, _dp, C.c_uint64, _P(C.c_uint64)]),
     "rrsph_status": (C.c_int, [C.c_void_p, _u32p, C.c_int]),
+    "rrsph_diagnostics_get": (C.c_int, [C.c_void_p, _P(RrsphDiagnostics)]),
     "rrsph_get_dt": (C.c_int, [C.c_void_p, _dp]),
     "rrsph_pair_count": (C.c_int, [C.c_void_p, _P(C.c_uint64), _P(C.c_uint64)]),
     "rrsph_grid_find": (C.c_int, [C.c_void_p, _u32p, _u32p, _u32p]),

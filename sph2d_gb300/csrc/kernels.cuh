@@ -149,6 +149,11 @@ struct HostReport {
     uint32_t flags;
 };
 void launch_set_time(StepScalars* scal, double time, uint32_t* flags, cudaStream_t st);
+// rrsph_diagnostics: blocks partial sums of kDiagQuantities doubles into part
+// (blocks * kDiagQuantities), then their fixed-order sum into out.
+constexpr int kDiagQuantities = 10;
+template <int DIM>
+void launch_diagnostics(const DevParams& P, const State& S, double* part, int blocks, double* out, cudaStream_t st);
 void launch_report(const StepScalars* scal, const uint32_t* flags, HostReport* out, cudaStream_t st);
 // Upload / download through device-addressable host arrays (pinned memory):
 // one kernel reading (writing) the caller's arrays over the host link. The

@@ -273,6 +273,68 @@ __global__ void k_upload_direct(DevParams P, State S, Sorted G, const double* __
     key_pass<DIM, 2>(P, S, G, i, S.rx[i], S.ry[i], DIM == 3 ? S.rz[i] : 0.0, flags);
 }
 
+// Global checks in double (rrsph_diagnostics): per fluid particle (itype > 0)
+// its mass, kinetic energy m|v|^2/2, potential energy m g y, the internal
+// energy m e(rho) of the Tait EOS p = B((rho/rho0)^7 - 1) — e(rho) the
+// integral of p/rho^2 from rho0, written with x = rho/rho0, t = x - 1 as
+// (B/rho0) t^2 (6 + 5x + 4x^2 + 3x^3 + 2x^4 + x^5) / (6x), free of
+// cancellation — and its momentum; per boundary particle (itype < 0) its mass.
+// Each block reduces a fixed set of particles in a fixed order and a second
+// kernel sums the blocks in a fixed order, so the result is the same every run.
+constexpr int kDiagQ = 10;  // mass, kinetic, potential, internal, px, py, pz, boundary mass, fluid, boundary
+constexpr int kDiagThreads = 256;
+
+template <int DIM>
+__global__ void __launch_bounds__(kDiagThreads) k_diag_blocks(DevParams P, State S, double* __restrict__ part) {
+    __shared__ double sh[kDiagQ][kDiagThreads];
+    double q[kDiagQ] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (uint32_t i = blockIdx.x * kDiagThreads + threadIdx.x; i < P.n; i += gridDim.x * kDiagThreads) {
+        const int32_t t = S.itype[i];
+        if (t > 0) {
+            const double vx = S.vx[i], vy = S.vy[i], vz = DIM == 3 ? S.vz[i] : 0.0;
+            const double x = S.rho[i] / P.rho0, tt = x - 1.0;
+            const double poly = 6.0 + x * (5.0 + x * (4.0 + x * (3.0 + x * (2.0 + x))));
+            q[0] += P.mass;
+            q[1] += 0.5 * P.mass * (vx * vx + vy * vy + vz * vz);
+            q[2] += P.mass * P.g * S.ry[i];
+            q[3] += P.mass * (P.B / P.rho0) * (tt * tt) * poly / (6.0 * x);
+            q[4] += P.mass * vx;
+            q[5] += P.mass * vy;
+            q[6] += P.mass * vz;
+            q[8] += 1.0;
+        } else if (t < 0) {
+            q[7] += P.mass;
+            q[9] += 1.0;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < kDiagQ; j++) sh[j][threadIdx.x] = q[j];
+    __syncthreads();
+    for (int w = kDiagThreads / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w)
+#pragma unroll
+            for (int j = 0; j < kDiagQ; j++) sh[j][threadIdx.x] += sh[j][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x < kDiagQ) part[(size_t)blockIdx.x * kDiagQ + threadIdx.x] = sh[threadIdx.x][0];
+}
+__global__ void __launch_bounds__(kDiagThreads) k_diag_sum(const double* __restrict__ part, int blocks,
+                                                           double* __restrict__ out) {
+    __shared__ double sh[kDiagThreads];
+    for (int j = 0; j < kDiagQ; j++) {
+        double v = 0.0;
+        for (int b = threadIdx.x; b < blocks; b += kDiagThreads) v += part[(size_t)b * kDiagQ + j];
+        sh[threadIdx.x] = v;
+        __syncthreads();
+        for (int w = kDiagThreads / 2; w > 0; w >>= 1) {
+            if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[j] = sh[0];
+        __syncthreads();
+    }
+}
+
 // rrsph_step's bookkeeping as kernels on the stream (no copy-engine round
 // trips): the time of the next step (and cleared status flags) before the
 // steps, the time and flags after them into a host mailbox.
@@ -308,6 +370,12 @@ __global__ void k_download_direct(DevParams P, State S, double* __restrict__ r, 
 inline int vec_layout(int dim, uint32_t stride, const void* a, const void* b) {
     const bool al = (reinterpret_cast<uintptr_t>(a) % 16 == 0) && (reinterpret_cast<uintptr_t>(b) % 16 == 0);
     return al && ((dim == 2 && stride == 2) || (dim == 3 && stride == 4)) ? 1 : 0;
+}
+
+template <int DIM>
+void launch_diagnostics(const DevParams& P, const State& S, double* part, int blocks, double* out, cudaStream_t st) {
+    k_diag_blocks<DIM><<<blocks, kDiagThreads, 0, st>>>(P, S, part);
+    k_diag_sum<<<1, kDiagThreads, 0, st>>>(part, blocks, out);
 }
 
 void launch_set_time(StepScalars* scal, double time, uint32_t* flags, cudaStream_t st) {
@@ -386,6 +454,7 @@ void launch_pack(const DevParams& P, State S, double* r, double* v, uint32_t str
                                            uint32_t*, cudaStream_t);                                           \
     template void launch_unpack<D>(const DevParams&, State, const double*, const double*, uint32_t, cudaStream_t); \
     template void launch_pack<D>(const DevParams&, State, double*, double*, uint32_t, cudaStream_t);         \
+    template void launch_diagnostics<D>(const DevParams&, const State&, double*, int, double*, cudaStream_t);  \
     template void launch_upload_direct<D>(const DevParams&, const State&, const Sorted&, const double*,        \
                                           const double*, const double*, const double*, const int32_t*,         \
                                           uint32_t, StepScalars*, double, uint32_t*, cudaStream_t);            \

@@ -828,6 +828,34 @@ extern "C" int rrsph_status(rrsph_solver* s, uint32_t* flags, int clear) {
     return RRSPH_OK;
 }
 
+extern "C" int rrsph_diagnostics_get(rrsph_solver* s, rrsph_diagnostics* out) {
+    int rc = check_handle(s, "rrsph_diagnostics_get");
+    if (rc) return rc;
+    if (!out) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_diagnostics_get: null output");
+    constexpr int kBlocks = 608;  // fixed: the summation order does not depend on the device
+    if (!s->diag) {
+        if ((rc = dev_alloc(s, &s->diag, (size_t)(kBlocks + 1) * rrsph::kDiagQuantities)) != 0) return rc;
+    }
+    double* sums = s->diag + (size_t)kBlocks * rrsph::kDiagQuantities;
+    if (s->dim == 3) rrsph::launch_diagnostics<3>(s->P, s->S, s->diag, kBlocks, sums, s->stream);
+    else rrsph::launch_diagnostics<2>(s->P, s->S, s->diag, kBlocks, sums, s->stream);
+    s->launches += 2;
+    double h[rrsph::kDiagQuantities];
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
+    RRSPH_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    out->mass = h[0];
+    out->kinetic = h[1];
+    out->potential = h[2];
+    out->internal = h[3];
+    out->momentum[0] = h[4];
+    out->momentum[1] = h[5];
+    out->momentum[2] = h[6];
+    out->mass_boundary = h[7];
+    out->fluid = (uint64_t)h[8];
+    out->boundary = (uint64_t)h[9];
+    return RRSPH_OK;
+}
+
 extern "C" int rrsph_pair_count(rrsph_solver* s, uint64_t* last_step, uint64_t* total) {
     int rc = check_handle(s, "rrsph_pair_count");
     if (rc) return rc;

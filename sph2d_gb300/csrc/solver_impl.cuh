@@ -34,6 +34,7 @@ struct rrsph_solver {
     uint32_t* h_flags = nullptr;           // pinned
     rrsph::HostReport* h_report = nullptr;  // mapped pinned mailbox of k_report
     rrsph::HostReport* d_report = nullptr;  // its device address
+    double* diag = nullptr;                 // rrsph_diagnostics_get: block partials, then the sums
     double* staging = nullptr;
     size_t staging_words = 0;
     std::vector<void*> allocations;

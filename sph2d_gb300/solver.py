@@ -171,6 +171,15 @@ class Solver:
         check(lib().rrsph_status(self._h, C.byref(f), 1 if clear else 0))
         return f.value
 
+    def diagnostics(self) -> dict:
+        """The double-precision mass and energy checks of the current state
+        (rrsph_diagnostics_get)."""
+        d = capi.RrsphDiagnostics()
+        check(lib().rrsph_diagnostics_get(self._h, C.byref(d)))
+        return {"mass": d.mass, "kinetic": d.kinetic, "potential": d.potential, "internal": d.internal,
+                "momentum": list(d.momentum), "mass_boundary": d.mass_boundary, "fluid": int(d.fluid),
+                "boundary": int(d.boundary)}
+
     def pair_count(self):
         """(pairs of the last step, pairs summed since upload)."""
         a, b = C.c_uint64(), C.c_uint64()

@@ -668,3 +668,50 @@ def test_neighbour_reuse_in_3d_and_with_continuity_density(gpu_available, dim, c
             runs.append(s.download())
     for k in ("r", "v", "rho", "p"):
         assert np.array_equal(runs[0][k], runs[1][k]), k
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_mass_and_energy_checks(gpu_available, precision, dim):
+    """rrsph_diagnostics_get against numpy sums of the downloaded state (the
+    summation orders differ, so to rounding), the same bits on every call,
+    the mass unchanged by the steps, non-existent particles left out."""
+    from sph2d_gb300 import Solver, cases
+
+    case = _dam(nx=40, ny=20) if dim == 2 else cases.dam_break_3d(dx=0.02, block=(0.2, 0.3, 0.2))
+    p = case.params()
+    c0, rho0 = case.notes["c0"], 1000.0
+    B = c0 * c0 * rho0 / 7.0
+    itype = case.itype.copy()
+    itype[:3] = 0  # three non-existent particles
+    with Solver(p, precision) as s:
+        s.upload(case.r, case.v, case.rho, itype)
+        d0 = s.diagnostics()
+        assert s.diagnostics() == d0
+        s.step(10, 0.0)
+        d1 = s.diagnostics()
+        assert d1 == s.diagnostics()
+        st = s.download()
+    assert d1["mass"] == d0["mass"] and d1["mass_boundary"] == d0["mass_boundary"]
+    fl, bd = st["itype"] > 0, st["itype"] < 0
+    m = p.mass
+    assert d1["fluid"] == int(fl.sum()) == int((case.itype > 0).sum()) - 3
+    assert d1["boundary"] == int(bd.sum())
+    v, r, rho = st["v"][fl], st["r"][fl], st["rho"][fl]
+    x = rho / rho0
+    t = x - 1.0
+    poly = 6.0 + x * (5.0 + x * (4.0 + x * (3.0 + x * (2.0 + x))))
+    want = {
+        "mass": m * fl.sum(),
+        "kinetic": 0.5 * m * float((v * v).sum()),
+        "potential": m * p.g * float(r[:, 1].sum()),
+        "internal": m * (B / rho0) * float((t * t * poly / (6.0 * x)).sum()),
+        "mass_boundary": m * bd.sum(),
+    }
+    for k, w in want.items():
+        assert abs(d1[k] - w) <= 1e-11 * max(abs(w), 1e-30), (k, d1[k], w)
+    mom = m * v.sum(axis=0)
+    for a in range(dim):
+        assert abs(d1["momentum"][a] - mom[a]) <= 1e-11 * max(abs(mom).max(), 1e-30), a
+    if dim == 2:
+        assert d1["momentum"][2] == 0.0
