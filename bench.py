@@ -199,6 +199,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     sm.step_async(args.warmup)
     sm.sync()
     clocks = ClockSampler(local_rank)
+    diag0 = sm.diagnostics()
     launches0 = sm.kernel_launches()
     rebuilds0 = sm.neighbour_rebuilds()
     _, pairs0 = sm.pair_count()
@@ -213,6 +214,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         dist.barrier()
     launches = sm.kernel_launches() - launches0
     rebuilds = sm.neighbour_rebuilds() - rebuilds0
+    diag1 = sm.diagnostics()
     last_pairs, pairs1 = sm.pair_count()
     pairs_timed = pairs1 - pairs0
     phases_mixed = _phase_pass(sm, flush, min(args.steps, 50))
@@ -338,6 +340,13 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": e2e_steps, "path": "rrsph_upload + rrsph_step(1) + rrsph_download, pinned host buffers"},
         "gpu_launches": launches,
+        "checks": {
+            "fluid_mass_exact": diag1["mass"] == diag0["mass"],
+            "fluid_mass": diag1["mass"],
+            "energy_before": {k: diag0[k] for k in ("kinetic", "potential", "internal")},
+            "energy_after": {k: diag1[k] for k in ("kinetic", "potential", "internal")},
+            "note": "rrsph_diagnostics_get before and after the timed steps (double, fixed-order sums)",
+        },
         "neighbour_rebuilds": {"timed_steps": args.steps, "rebuilds": rebuilds,
                                "note": "grid + candidate lists rebuilt when a particle moved half the 0.3 h skin"},
         "clocks": clocks_info,
