@@ -17,7 +17,7 @@ namespace rrsph {
 namespace {
 
 constexpr int kVlBatch = 4;       // list entries the density gather loads together (one uint4)
-constexpr int kVlForceBatch = 2;  // neighbours the force gather loads together
+constexpr int kVlForceBatch = 4;  // neighbours the force gather loads together
 
 // List entry = sorted index | cell code << Vl<DIM>::shift, with the code of
 // the candidate's cell offset (dx, dy[, dz]) in [-2, 2]^dim:
