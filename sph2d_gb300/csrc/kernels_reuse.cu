@@ -201,6 +201,8 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
                                                                      uint32_t* __restrict__ flags) {
     constexpr int CAP = Vl<DIM>::cap;
     constexpr uint32_t IDX = Vl<DIM>::index;
+    // the force gather may launch now: it waits for this grid at its start (griddepcontrol.wait)
+    asm volatile("griddepcontrol.launch_dependents;");
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = k < P.n;
     uint32_t cnt = 0;
@@ -337,6 +339,8 @@ __global__ void __launch_bounds__(kMaxGatherThreads, 4) k_forces_verlet(DevParam
                                                                     StepScalars* __restrict__ next,
                                                                     uint32_t* __restrict__ flags) {
     constexpr uint32_t IDX = Vl<DIM>::index;
+    // launched while the density gather finishes: wait for it (and its writes) first
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = k < P.n;
     double amag = 0, arvmu_d = 0;
@@ -508,6 +512,23 @@ void launch_density_verlet(const DevParams& P, const State& S, const Sorted& G, 
         else k_density_verlet<DIM, 0, false><<<blocks, threads, 0, st>>>(P, S, G, scal, flags);
     }
 }
+// A launch that may start while the stream's previous kernel finishes
+// (programmatic dependent launch); the kernel waits for it with
+// griddepcontrol.wait before it reads what that kernel wrote.
+template <typename... Params, typename... Args>
+void launch_after(void (*kernel)(Params...), unsigned blocks, int threads, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 template <int DIM>
 void launch_forces_verlet(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal,
                           StepScalars* scal_next, uint32_t* flags, cudaStream_t st, int threads, int whole) {
@@ -517,30 +538,25 @@ void launch_forces_verlet(const DevParams& P, const State& S, const Sorted& G, S
     const int wv = whole ? (kVarMixed | (P.density_treatment != 0 ? kVarCont : 0) |
                             (P.avg_vel || P.dt_method == 2 ? kVarRare : 0))
                          : 0;
-#define RRSPH_FV(SKF, STD)                                                                                        \
-    do {                                                                                                          \
-        switch (wv) {                                                                                             \
-        case 0: k_forces_verlet<DIM, SKF, STD, 0><<<blocks, threads, 0, st>>>(P, S, G, scal, scal_next, flags);   \
-            break;                                                                                                \
-        case kVarMixed:                                                                                           \
-            k_forces_verlet<DIM, SKF, STD, kVarMixed><<<blocks, threads, 0, st>>>(P, S, G, scal, scal_next, flags); \
-            break;                                                                                                \
-        case kVarMixed | kVarCont:                                                                                \
-            k_forces_verlet<DIM, SKF, STD, kVarMixed | kVarCont><<<blocks, threads, 0, st>>>(P, S, G, scal,        \
-                                                                                           scal_next, flags);    \
-            break;                                                                                                \
-        case kVarMixed | kVarRare:                                                                                \
-            k_forces_verlet<DIM, SKF, STD, kVarMixed | kVarRare><<<blocks, threads, 0, st>>>(P, S, G, scal,        \
-                                                                                           scal_next, flags);    \
-            break;                                                                                                \
-        default:                                                                                                  \
-            k_forces_verlet<DIM, SKF, STD, kVarMixed | kVarCont | kVarRare><<<blocks, threads, 0, st>>>(           \
-                P, S, G, scal, scal_next, flags);                                                                 \
-        }                                                                                                         \
+// the force gather follows the density gather with a programmatic dependency:
+// its blocks launch as the density gather's last blocks run, then wait for it
+#define RRSPH_FV(SKF, STD, WV) \
+    launch_after(k_forces_verlet<DIM, SKF, STD, WV>, blocks, threads, st, P, S, G, scal, scal_next, flags)
+#define RRSPH_FV_WV(SKF, STD)                                                          \
+    do {                                                                               \
+        switch (wv) {                                                                  \
+        case 0: RRSPH_FV(SKF, STD, 0); break;                                          \
+        case kVarMixed: RRSPH_FV(SKF, STD, kVarMixed); break;                          \
+        case kVarMixed | kVarCont: RRSPH_FV(SKF, STD, kVarMixed | kVarCont); break;    \
+        case kVarMixed | kVarRare: RRSPH_FV(SKF, STD, kVarMixed | kVarRare); break;    \
+        default: RRSPH_FV(SKF, STD, kVarMixed | kVarCont | kVarRare);                  \
+        }                                                                              \
     } while (0)
-    if (DIM == 2 && std_terms) RRSPH_FV(1, (DIM == 2));
-    else if (P.all_cubic) RRSPH_FV(1, false);
-    else RRSPH_FV(0, false);
+    if (DIM == 2 && std_terms) RRSPH_FV_WV(1, (DIM == 2));
+    else if (P.all_cubic) RRSPH_FV_WV(1, false);
+    else RRSPH_FV_WV(0, false);
+#undef RRSPH_FV_WV
+#undef RRSPH_FV
 #undef RRSPH_FV
 }
 
