@@ -557,7 +557,6 @@ void launch_forces_verlet(const DevParams& P, const State& S, const Sorted& G, S
     else RRSPH_FV_WV(0, false);
 #undef RRSPH_FV_WV
 #undef RRSPH_FV
-#undef RRSPH_FV
 }
 
 template void launch_verlet_build<2>(const DevParams&, const State&, const Sorted&, cudaStream_t);
