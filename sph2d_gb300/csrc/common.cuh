@@ -74,7 +74,7 @@ struct DevParams {
     int dt_reduce;          // 1: true max reduction
     double cfl, never_ending_dt;
     int all_cubic;          // every smoothing kernel choice is the cubic spline
-    // neighbour reuse (2D mixed): list cutoff (cell + skin)^2, (skin / 2)^2, and
+    // neighbour reuse (mixed step): list cutoff (cell + skin)^2, (skin / 2)^2, and
     // the distance from a cell edge within which the list looks two cells away
     float vl_cut2, vl_half_skin2, vl_skin_edge;
     MixedF mf;

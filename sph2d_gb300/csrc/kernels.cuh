@@ -114,7 +114,7 @@ template <int DIM>
 void launch_whole_step(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal_cur,
                        StepScalars* scal_next, uint32_t* flags, int next_keys, cudaStream_t st);
 
-// Neighbour reuse (2D mixed step with summation density): the candidate lists
+// Neighbour reuse (the FP32-mixed step): the candidate lists
 // are built with the cutoff widened by a skin and reused while no particle has
 // moved more than half the skin since the build (kernels_reuse.cu).
 void launch_verlet_decide(cudaGraphConditionalHandle h, const uint32_t* rebuild, cudaStream_t st);

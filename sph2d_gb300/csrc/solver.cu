@@ -272,7 +272,7 @@ void enqueue_verlet_rebuild(rrsph_solver* s, cudaStream_t st) {
     s->launches += 3;
 }
 
-// One step of the 2D mixed loop with neighbour reuse. In a captured graph the
+// One step of the mixed loop with neighbour reuse. In a captured graph the
 // rebuild is a conditional node that a kernel sets from the flag the last key
 // pass raised; with direct launches the host reads the flag.
 int enqueue_step_verlet(rrsph_solver* s, int par, cudaEvent_t* events, bool with_keys) {

@@ -51,7 +51,7 @@ struct rrsph_solver {
     uint64_t timed_steps = 0;
     rrsph_impl::AdjointRun* adj = nullptr;
     int gather_threads[2] = {rrsph::kGatherThreads, rrsph::kGatherThreads};  // density, forces block sizes
-    // neighbour reuse of the 2D FP32-mixed step (summation density)
+    // neighbour reuse of the FP32-mixed step
     bool verlet = false;
     double verlet_skin = 0.3;                  // skin, in units of hsml
     cudaStream_t aux = nullptr;                // captures the rebuild / reuse bodies of a step graph

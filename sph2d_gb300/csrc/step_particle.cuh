@@ -1,7 +1,7 @@
 // step_particle.cuh — the per-particle pieces of the time step that more than
 // one kernel runs: the geometry test, the key pass, predict_half_step, the
 // piston laws and the whole step of one particle. The whole-step kernel runs
-// them over all particles; the fused force + whole-step gather of the 2D mixed
+// them over all particles; the fused force + whole-step gather of the mixed
 // step with neighbour reuse runs them for the particle whose acceleration it
 // has just summed.
 #pragma once

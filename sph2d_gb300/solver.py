@@ -240,7 +240,7 @@ class Solver:
         return int(out[0]), int(out[1])
 
     def set_neighbour_reuse(self, enable: bool, skin_over_h: float = 0.3) -> None:
-        """Candidate-list reuse of the 2D mixed step (summation density)."""
+        """Candidate-list reuse of the FP32-mixed step (2D or 3D, summation or continuity density)."""
         check(lib().rrsph_set_neighbour_reuse(self._h, 1 if enable else 0, float(skin_over_h)))
 
     def neighbour_rebuilds(self) -> int:
