@@ -65,6 +65,15 @@ __device__ __forceinline__ float kernel_dwdr_scalef(int skf, float f, float q, f
     }
 }
 
+// The cubic dW/dr scale of kernel_dwdr_scalef as selects (both branches of the
+// spline evaluated, no divergence between the lanes of a warp).
+__device__ __forceinline__ float cubic_dwdr_sel(float f, float q, float inv_dist, float inv_h) {
+    const float t = 2.0f - q;
+    const float s1 = inv_h * inv_h * f * (-2.0f + 1.5f * q);
+    const float s2 = -(inv_h * inv_dist) * f * (t * t * 0.5f);
+    return q <= 1.0f ? s1 : (q <= 2.0f ? s2 : 0.0f);
+}
+
 // Cutoff test: float test outside the guard band, the reference's double test inside it.
 // The guard band is rare, so its double positions come from the id-order state.
 template <int DIM>
@@ -178,7 +187,7 @@ struct ForceAcc {
         float m = 0.0f;
         if (ext && ti < 0 && dist < M.lj_rr0) m -= lj_coef(M, inv_dist);
         const float rhoi = vi.w;
-        const float sc = kernel_dwdr_scalef(1, M.kf[1], q, inv_dist, M.inv_h);
+        const float sc = cubic_dwdr_sel(M.kf[1], q, inv_dist, M.inv_h);
         m += sc * (vi.z + prj.y) * M.mass;
         const float vr = -((vj.x - vi.x) * dx + (vj.y - vi.y) * dy);
         const float mu = fminf(__fdividef(M.h * vr, d2 + M.etq_h2), 0.0f);
