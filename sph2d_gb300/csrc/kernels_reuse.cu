@@ -17,7 +17,10 @@ namespace rrsph {
 namespace {
 
 constexpr int kVlBatch = 4;       // list entries the density gather loads together (one uint4)
-constexpr int kVlForceBatch = 4;  // neighbours the force gather loads together
+// neighbours the force gather loads together: four for the 2D common method
+// set, two elsewhere (four would spill the registers of the general pair)
+template <int DIM, bool STD>
+constexpr int kVlForceBatch = DIM == 2 && STD ? 4 : 2;
 
 // List entry = sorted index | cell code << Vl<DIM>::shift, with the code of
 // the candidate's cell offset (dx, dy[, dz]) in [-2, 2]^dim:
@@ -373,14 +376,14 @@ __global__ void __launch_bounds__(kMaxGatherThreads, 4) k_forces_verlet(DevParam
                     const uint4 w = __ldcs(nslab + (size_t)(e0 >> 2) * P.n);  // streaming, as in the density pass
                     const uint32_t eg[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
-                    for (int h = 0; h < 4; h += kVlForceBatch) {
-                        uint32_t en[kVlForceBatch];
-                        float4 pb[kVlForceBatch], vb[kVlForceBatch];
-                        float2 rb[kVlForceBatch];
+                    for (int h = 0; h < 4; h += kVlForceBatch<DIM, STD>) {
+                        uint32_t en[kVlForceBatch<DIM, STD>];
+                        float4 pb[kVlForceBatch<DIM, STD>], vb[kVlForceBatch<DIM, STD>];
+                        float2 rb[kVlForceBatch<DIM, STD>];
 #pragma unroll
-                        for (int j = 0; j < kVlForceBatch; j++) en[j] = e0 + h + j < nc ? eg[h + j] : kVlNone;
+                        for (int j = 0; j < kVlForceBatch<DIM, STD>; j++) en[j] = e0 + h + j < nc ? eg[h + j] : kVlNone;
 #pragma unroll
-                        for (int j = 0; j < kVlForceBatch; j++) {
+                        for (int j = 0; j < kVlForceBatch<DIM, STD>; j++) {
                             if (en[j] == kVlNone) continue;
                             const uint32_t i = en[j] & IDX;
                             pb[j] = G.P4[i];
@@ -390,7 +393,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads, 4) k_forces_verlet(DevParam
                         // each pair's terms are added with compensation (no per-cell
                         // partial sums, whose flushes would split the warp)
 #pragma unroll
-                        for (int j = 0; j < kVlForceBatch; j++) {
+                        for (int j = 0; j < kVlForceBatch<DIM, STD>; j++) {
                             if (en[j] == kVlNone) continue;
                             uint32_t cx, cy, cz;
                             vl_offset<DIM>(en[j], cx, cy, cz);
