@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
                         if (in) nslab[(size_t)(cnt >> 2) * 4 * P.n + (cnt & 3u)] = en[j];
                         cnt += in;
                     }
-                    acc.add(CONT ? M.mass * part : M.mass * part);
+                    acc.add(M.mass * part);
                     w = wn;
                 }
             } else {
@@ -555,6 +555,8 @@ void launch_forces_verlet(const DevParams& P, const State& S, const Sorted& G, S
         default: RRSPH_FV(SKF, STD, kVarMixed | kVarCont | kVarRare);                  \
         }                                                                              \
     } while (0)
+    // STD = DIM == 2: the common-method variant exists in 2D only (std_terms is
+    // false in 3D), so no 3D instance of it is compiled
     if (DIM == 2 && std_terms) RRSPH_FV_WV(1, (DIM == 2));
     else if (P.all_cubic) RRSPH_FV_WV(1, false);
     else RRSPH_FV_WV(0, false);
