@@ -746,3 +746,33 @@ def test_neighbour_reuse_with_every_method_switch(gpu_available, sw):
     assert pa == pb
     for k in ("r", "v", "rho"):
         assert rel_l2(a[k], b[k]) < 1e-5, (k, rel_l2(a[k], b[k]))
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_neighbour_reuse_with_delta_sph(gpu_available, dim):
+    """Continuity density with the delta-SPH term through candidate-list
+    reuse against the per-step stencil search."""
+    from sph2d_gb300 import Solver, cases
+
+    if dim == 2:
+        case = _dam(nx=50, ny=25, density_treatment=1)
+    else:
+        case = cases.dam_break_3d(dx=0.02, block=(0.3, 0.3, 0.3), density_treatment=1)
+    p = case.params()
+    p.density_treatment = 2
+    p.density_delta_sph_coef = 0.1
+    out = []
+    for reuse in (True, False):
+        with Solver(p, "mixed") as s:
+            s.set_neighbour_reuse(reuse)
+            s.upload(case.r, case.v, case.rho, case.itype)
+            pairs = []
+            t = 0.0
+            for _ in range(20):
+                t = s.step(1, t)
+                pairs.append(s.pair_count()[0])
+            out.append((s.download(), pairs))
+    (a, pa), (b, pb) = out
+    assert pa == pb
+    for k in ("r", "v", "rho"):
+        assert rel_l2(a[k], b[k]) < 1e-5, (k, rel_l2(a[k], b[k]))
