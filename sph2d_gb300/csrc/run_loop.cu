@@ -22,6 +22,7 @@
 #include <cstring>
 #include <deque>
 #include <filesystem>
+#include <limits>
 #include <functional>
 #include <mutex>
 #include <string>
@@ -149,7 +150,8 @@ extern "C" int rrsph_run(rrsph_solver* s, const char* experiment_dir, double* ti
     double dt = p.dt;
     if (p.dt_correction_method == 2 && !p.dt_dynamic_reduce) {
         const double c_sqr = p.eos_sound_vel_method == 0 ? 200 * p.g * p.depth * p.eos_sound_vel_coef : p.eos_sound_vel;
-        dt = p.CFL_coef * std::min(std::sqrt(p.hsml / 0.0), p.hsml / (std::sqrt(c_sqr) + 0.0));
+        // update_dt(0, 0) of the OMP build: sqrt(h / 0) is +inf, so the sound speed decides
+        dt = p.CFL_coef * std::min(std::numeric_limits<double>::infinity(), p.hsml / (std::sqrt(c_sqr) + 0.0));
     }
     const unsigned nthreads = std::max(1u, std::min(8u, std::thread::hardware_concurrency() / 2));
     Writers writers(p, nthreads);

@@ -331,7 +331,8 @@ int enqueue_step_verlet(rrsph_solver* s, int par, cudaEvent_t* events, bool with
     if (events) cudaEventRecord(events[4], st);
     // the whole step runs inside the force gather unless dt waits for the step's
     // maxima or a particle may have more neighbours than a list holds
-    const bool fuse = !(s->P.dt_method == 2 && s->P.dt_reduce) && s->P.max_nb <= rrsph::verlet_cap(s->dim) + 1;
+    const bool fuse = !(s->P.dt_method == 2 && s->P.dt_reduce) &&
+                      s->P.max_nb <= (uint32_t)rrsph::verlet_cap(s->dim) + 1u;
     if (d3) rrsph::launch_forces_verlet<3>(s->P, s->S, s->G, cur, nxt, s->flags, st, s->gather_threads[1], fuse ? 1 : 0);
     else rrsph::launch_forces_verlet<2>(s->P, s->S, s->G, cur, nxt, s->flags, st, s->gather_threads[1], fuse ? 1 : 0);
     if (events) cudaEventRecord(events[5], st);
