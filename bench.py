@@ -376,6 +376,8 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         result["ensemble"] = ensemble_measure()
     if rank == 0 and world == 1 and not args.no_dam3d:
         result["dam_break_3d"] = dam3d_measure()
+    if rank == 0 and world == 1 and not args.no_output:
+        result["output_io"] = output_measure()
     if rank == 0 and world == 1 and not args.no_adjoint:
         result["adjoint"] = adjoint_measure(steps=args.adjoint_steps)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -447,6 +449,50 @@ def ensemble_measure(steps: int = 50, seq_steps: int = 10, ntanks: int = 256) ->
         "sequential": {"ms_per_step": seq_ms, "pair_interactions_per_s": seq_rate, "steps_per_tank": seq_steps},
         "speedup": seq_ms / (ms / steps),
         "launches_in_batched_region": launches,
+    }
+
+
+def output_measure(steps: int = 400, every: int = 100) -> dict:
+    """The flume's FP32-mixed step with the reference's layer output
+    (rrsph_run: a data layer every `every` steps, formatted by writer threads
+    while the next steps run) against the same steps without output; wall
+    time of the whole call, as a user sees it."""
+    import shutil
+    import tempfile
+
+    import torch
+
+    from sph2d_gb300 import Solver, cases
+
+    case = cases.piston_flume_2d()
+    p = case.params()
+    p.save_time = every * p.dt
+    p.simulation_time = steps * p.dt
+    d = tempfile.mkdtemp(prefix="rrsph_run_")
+    try:
+        with Solver(p, "mixed") as s:
+            s.upload(case.r, case.v, case.rho, case.itype)
+            s.step(3, 0.0)  # graph capture and first build
+            s.upload(case.r, case.v, case.rho, case.itype)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            _, n = s.run(d, 0.0)
+            wall_out = time.perf_counter() - t0
+            s.upload(case.r, case.v, case.rho, case.itype)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s.step(n, 0.0)
+            wall_plain = time.perf_counter() - t0
+        layers = sorted((Path(d) / "data").glob("*.csv"))
+        size = sum(f.stat().st_size for f in layers)
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    return {
+        "workload": f"2D piston flume, {case.ntotal} particles, {n} steps, a data layer (CSV, 6 decimals) every {every} "
+                    "steps as RRSPHOutput writes them",
+        "with_output": {"ms_per_step": wall_out / n * 1e3, "layers": len(layers), "layer_bytes": size},
+        "without_output": {"ms_per_step": wall_plain / n * 1e3},
+        "timing": "wall clock of rrsph_run / rrsph_step over the whole call",
     }
 
 
@@ -635,6 +681,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 256-tank ensemble measurement")
     ap.add_argument("--no-dam3d", action="store_true", help="skip the 3D dam break measurement")
+    ap.add_argument("--no-output", action="store_true", help="skip the run with layer output")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost measurement")
     ap.add_argument("--adjoint-steps", type=int, default=500)
     args = ap.parse_args()

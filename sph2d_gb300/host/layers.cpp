@@ -13,7 +13,9 @@
 #include <cstdlib>
 #include <cstring>
 #include <filesystem>
+#include <algorithm>
 #include <string>
+#include <thread>
 #include <vector>
 
 using rrsph::set_error;
@@ -135,35 +137,48 @@ extern "C" int rrsph_layer_write(const char* csv_path, const rrsph_params* p, co
     const bool wp = dump ? true : (p->save_pressure && pres);
     if ((wv && !v) || (wr && !rho) || (wp && !pres))
         return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_layer_write: a dump needs r, itype, v, rho and p");
-    std::string out;
-    out.reserve((size_t)p->ntotal * 96 + 64);
-    out += d3 ? "x,y,z,itype" : "x,y,itype";
-    if (wv) out += d3 ? ",vx,vy,vz" : ",vx,vy";
-    if (wr) out += ",rho";
-    if (wp) out += ",p";
-    out += '\n';
-    char ibuf[32];
-    for (uint64_t i = 0; i < p->ntotal; i++) {
-        const double* ri = r + i * stride;
-        put_f(out, ri[0]); out += ',';
-        put_f(out, ri[1]); out += ',';
-        if (d3) { put_f(out, ri[2]); out += ','; }
-        const int n = std::snprintf(ibuf, sizeof(ibuf), "%ld", (long)itype[i]);
-        out.append(ibuf, (size_t)n);
-        if (wv) {
-            const double* vi = v + i * stride;
-            out += ','; put_f(out, vi[0]);
-            out += ','; put_f(out, vi[1]);
-            if (d3) { out += ','; put_f(out, vi[2]); }
+    std::string head = d3 ? "x,y,z,itype" : "x,y,itype";
+    if (wv) head += d3 ? ",vx,vy,vz" : ",vx,vy";
+    if (wr) head += ",rho";
+    if (wp) head += ",p";
+    head += '\n';
+    // the lines of particles [i0, i1) into out
+    auto lines = [&](uint64_t i0, uint64_t i1, std::string& out) {
+        out.reserve((size_t)(i1 - i0) * 96);
+        char ibuf[32];
+        for (uint64_t i = i0; i < i1; i++) {
+            const double* ri = r + i * stride;
+            put_f(out, ri[0]); out += ',';
+            put_f(out, ri[1]); out += ',';
+            if (d3) { put_f(out, ri[2]); out += ','; }
+            const auto res = std::to_chars(ibuf, ibuf + sizeof(ibuf), (long)itype[i]);
+            out.append(ibuf, (size_t)(res.ptr - ibuf));
+            if (wv) {
+                const double* vi = v + i * stride;
+                out += ','; put_f(out, vi[0]);
+                out += ','; put_f(out, vi[1]);
+                if (d3) { out += ','; put_f(out, vi[2]); }
+            }
+            if (wr) { out += ','; put_f(out, rho[i]); }
+            if (wp) { out += ','; put_f(out, pres[i]); }
+            out += '\n';
         }
-        if (wr) { out += ','; put_f(out, rho[i]); }
-        if (wp) { out += ','; put_f(out, pres[i]); }
-        out += '\n';
-    }
+    };
+    // contiguous ranges formatted in parallel, written in order (the same bytes)
+    const uint64_t n = p->ntotal;
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const uint64_t parts = std::max<uint64_t>(1, std::min<uint64_t>({(uint64_t)std::min(hw, 8u), n / 16384}));
+    std::vector<std::string> chunk(parts);
+    std::vector<std::thread> pool;
+    for (uint64_t c = 1; c < parts; c++)
+        pool.emplace_back([&, c] { lines(n * c / parts, n * (c + 1) / parts, chunk[c]); });
+    lines(0, n / parts, chunk[0]);
+    for (auto& t : pool) t.join();
     FILE* f = std::fopen(csv_path, "wb");
     if (!f) return set_error(RRSPH_ERR_IO, std::string("cannot write layer ") + csv_path);
-    const size_t put = std::fwrite(out.data(), 1, out.size(), f);
+    bool ok = std::fwrite(head.data(), 1, head.size(), f) == head.size();
+    for (const auto& c : chunk) ok = ok && std::fwrite(c.data(), 1, c.size(), f) == c.size();
     std::fclose(f);
-    if (put != out.size()) return set_error(RRSPH_ERR_IO, std::string("short write of layer ") + csv_path);
+    if (!ok) return set_error(RRSPH_ERR_IO, std::string("short write of layer ") + csv_path);
     return RRSPH_OK;
 }
