@@ -53,17 +53,111 @@ std::string time_digits(double time, int digits) {
     return buf;
 }
 
+// One layer's arrays in one host block.
+struct Block {
+    char* data = nullptr;
+    bool pinned = false;
+};
+
+// Host blocks for the layers in flight. Up to max_pinned of them are
+// page-locked and kept for reuse (rrsph_download then writes them with one
+// kernel over the host link); past that, pageable blocks are allocated and
+// freed per layer (rrsph_download copies into them through a staging buffer).
+class BlockPool {
+public:
+    BlockPool(size_t bytes, size_t max_pinned) : bytes_(bytes), max_pinned_(max_pinned) {}
+    BlockPool(const BlockPool&) = delete;
+    BlockPool& operator=(const BlockPool&) = delete;
+    ~BlockPool() {
+        for (const Block& b : free_) cudaFreeHost(b.data);
+    }
+    size_t bytes() const { return bytes_; }
+    Block get() {
+        {
+            std::lock_guard<std::mutex> lock(mu_);
+            if (!free_.empty()) {
+                const Block b = free_.back();
+                free_.pop_back();
+                return b;
+            }
+            if (pinned_ < max_pinned_) {
+                void* q = nullptr;
+                if (cudaMallocHost(&q, bytes_) == cudaSuccess) {
+                    pinned_++;
+                    return {static_cast<char*>(q), true};
+                }
+                cudaGetLastError();
+                max_pinned_ = pinned_;  // no more page-locked memory: stop asking
+            }
+        }
+        return {static_cast<char*>(std::malloc(bytes_)), false};
+    }
+    void put(const Block& b) {
+        if (!b.data) return;
+        if (!b.pinned) {
+            std::free(b.data);
+            return;
+        }
+        std::lock_guard<std::mutex> lock(mu_);
+        free_.push_back(b);
+    }
+
+private:
+    const size_t bytes_;
+    size_t max_pinned_;
+    size_t pinned_ = 0;
+    std::mutex mu_;
+    std::vector<Block> free_;
+};
+
+// Byte offsets of the arrays in a block (16-byte aligned starts).
+struct LayerShape {
+    size_t n, dim, r, v, rho, p, itype, bytes;
+    LayerShape(size_t n_, size_t dim_) : n(n_), dim(dim_) {
+        auto up = [](size_t x) { return (x + 15) & ~size_t(15); };
+        r = 0;
+        v = up(r + n * dim * sizeof(double));
+        rho = up(v + n * dim * sizeof(double));
+        p = up(rho + n * sizeof(double));
+        itype = up(p + n * sizeof(double));
+        bytes = up(itype + n * sizeof(int32_t));
+    }
+};
+
+// A layer on its way to a file: the arrays (in a pool block) and the path.
 struct Layer {
-    std::vector<double> r, v, rho, p;
-    std::vector<int32_t> itype;
+    BlockPool* pool = nullptr;
+    Block block;
     std::string path;
     bool dump = false;
+    Layer() = default;
+    Layer(const Layer&) = delete;
+    Layer& operator=(const Layer&) = delete;
+    Layer(Layer&& o) noexcept : pool(o.pool), block(o.block), path(std::move(o.path)), dump(o.dump) { o.block = {}; }
+    Layer& operator=(Layer&& o) noexcept {
+        if (this != &o) {
+            release();
+            pool = o.pool;
+            block = o.block;
+            path = std::move(o.path);
+            dump = o.dump;
+            o.block = {};
+        }
+        return *this;
+    }
+    ~Layer() { release(); }
+    void release() {
+        if (pool) pool->put(block);
+        block = {};
+    }
+    double* f64(size_t off) const { return reinterpret_cast<double*>(block.data + off); }
+    int32_t* i32(size_t off) const { return reinterpret_cast<int32_t*>(block.data + off); }
 };
 
 // Writer threads for the CSV layers.
 class Writers {
 public:
-    Writers(const rrsph_params& p, unsigned n) : params_(p) {
+    Writers(const rrsph_params& p, const LayerShape& shape, unsigned n) : params_(p), shape_(shape) {
         for (unsigned i = 0; i < n; i++) threads_.emplace_back([this] { loop(); });
     }
     ~Writers() { finish(); }
@@ -99,8 +193,10 @@ private:
                 queue_.pop_front();
                 room_.notify_one();
             }
-            const int rc = rrsph_layer_write(l.path.c_str(), &params_, l.r.data(), params_.dim, l.v.data(),
-                                             l.rho.data(), l.p.data(), l.itype.data(), l.dump ? 1 : 0);
+            const int rc = rrsph_layer_write(l.path.c_str(), &params_, l.f64(shape_.r), params_.dim,
+                                             l.f64(shape_.v), l.f64(shape_.rho), l.f64(shape_.p),
+                                             l.i32(shape_.itype), l.dump ? 1 : 0);
+            l.release();  // before the next layer is taken
             if (rc) {
                 std::lock_guard<std::mutex> lock(mu_);
                 if (!rc_) {
@@ -111,6 +207,7 @@ private:
         }
     }
     rrsph_params params_;
+    LayerShape shape_;
     std::mutex mu_;
     std::condition_variable cv_, room_;
     std::deque<Layer> queue_;
@@ -120,14 +217,24 @@ private:
     std::string err_;
 };
 
-int snapshot(rrsph_solver* s, Layer& l) {
-    const size_t n = s->params.ntotal, dim = s->params.dim;
-    l.r.resize(n * dim);
-    l.v.resize(n * dim);
-    l.rho.resize(n);
-    l.p.resize(n);
-    l.itype.resize(n);
-    return rrsph_download(s, l.r.data(), (uint32_t)dim, l.v.data(), l.rho.data(), l.p.data(), l.itype.data());
+// The current state into a fresh layer from the pool.
+int snapshot(rrsph_solver* s, BlockPool& pool, const LayerShape& sh, Layer& l) {
+    l.release();
+    l.pool = &pool;
+    l.block = pool.get();
+    if (!l.block.data) return set_error(RRSPH_ERR_OUT_OF_MEMORY, "rrsph_run: no host memory for a layer");
+    return rrsph_download(s, l.f64(sh.r), (uint32_t)sh.dim, l.f64(sh.v), l.f64(sh.rho), l.f64(sh.p),
+                          l.i32(sh.itype));
+}
+
+// A second layer with the same arrays.
+int copy_layer(BlockPool& pool, const LayerShape& sh, const Layer& from, Layer& to) {
+    to.release();
+    to.pool = &pool;
+    to.block = pool.get();
+    if (!to.block.data) return set_error(RRSPH_ERR_OUT_OF_MEMORY, "rrsph_run: no host memory for a layer");
+    std::memcpy(to.block.data, from.block.data, sh.bytes);
+    return RRSPH_OK;
 }
 
 }  // namespace
@@ -154,7 +261,10 @@ extern "C" int rrsph_run(rrsph_solver* s, const char* experiment_dir, double* ti
         dt = p.CFL_coef * std::min(std::numeric_limits<double>::infinity(), p.hsml / (std::sqrt(c_sqr) + 0.0));
     }
     const unsigned nthreads = std::max(1u, std::min(8u, std::thread::hardware_concurrency() / 2));
-    Writers writers(p, nthreads);
+    const LayerShape shape(p.ntotal, p.dim);
+    // page-locked blocks for the layers in flight, up to 1 GiB (at least two)
+    BlockPool pool(shape.bytes, std::max<size_t>(2, (size_t(1) << 30) / std::max<size_t>(shape.bytes, 1)));
+    Writers writers(p, shape, nthreads);  // after the pool: the writers finish before it goes
 
     double time = *time_io;
     double last_save = time, last_dump = time;
@@ -162,7 +272,7 @@ extern "C" int rrsph_run(rrsph_solver* s, const char* experiment_dir, double* ti
     int rc = RRSPH_OK;
     {   // first layer (setup_output)
         Layer l;
-        if ((rc = snapshot(s, l)) != 0) return rc;
+        if ((rc = snapshot(s, pool, shape, l)) != 0) return rc;
         l.path = (dir / "data" / (time_digits(time, save_digits) + ".csv")).string();
         writers.push(std::move(l));
     }
@@ -190,7 +300,7 @@ extern "C" int rrsph_run(rrsph_solver* s, const char* experiment_dir, double* ti
         if (rc == RRSPH_ERR_OUTSIDE_GEOMETRY) {
             if (p.use_crash_dump) {
                 Layer l;
-                if (snapshot(s, l) == RRSPH_OK) {
+                if (snapshot(s, pool, shape, l) == RRSPH_OK) {
                     l.path = (dir / ("crash_dump_" + time_digits(time, save_digits) + ".csv")).string();
                     l.dump = true;
                     writers.push(std::move(l));
@@ -201,9 +311,10 @@ extern "C" int rrsph_run(rrsph_solver* s, const char* experiment_dir, double* ti
         if (rc) break;
         if (save || dump) {
             Layer l;
-            if ((rc = snapshot(s, l)) != 0) break;
+            if ((rc = snapshot(s, pool, shape, l)) != 0) break;
             if (save && dump) {
-                Layer d = l;
+                Layer d;
+                if ((rc = copy_layer(pool, shape, l, d)) != 0) break;
                 d.path = (dir / "dump" / (time_digits(time, dump_digits) + ".csv")).string();
                 d.dump = true;
                 writers.push(std::move(d));

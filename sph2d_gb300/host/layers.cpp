@@ -9,6 +9,8 @@
 #include "error.hpp"
 
 #include <charconv>
+#include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -22,17 +24,53 @@ using rrsph::set_error;
 
 namespace {
 
-// std::to_string(double) is specified as printf("%f"); std::to_chars with
-// fixed format and precision 6 produces the same characters, faster.
-void put_f(std::string& out, double v) {
-    char buf[512];
-    const auto res = std::to_chars(buf, buf + sizeof(buf), v, std::chars_format::fixed, 6);
-    if (res.ec == std::errc()) {
-        out.append(buf, (size_t)(res.ptr - buf));
-    } else {
-        const int n = std::snprintf(buf, sizeof(buf), "%f", v);
-        out.append(buf, (size_t)(n > 0 ? n : 0));
+// std::to_string(double) is specified as printf("%f"): the exact binary value
+// rounded to 6 decimals, ties to even. For a finite |v| < 9e12 that is done
+// here with integers: v = m * 2^e (e < 0 in that range), and
+// q = m * 10^6 / 2^-e rounded half to even in 128-bit arithmetic is the value
+// in millionths, printed as q / 10^6 '.' q % 10^6 with six digits. The sign of
+// a negative value that rounds to zero (and of -0.0) is kept, as printf keeps
+// it. Other values (infinities, NaN, |v| >= 9e12) go to std::to_chars with
+// fixed format and precision 6, which is specified to match printf.
+// Writes at most kMaxNumberChars characters at o; returns the end.
+constexpr size_t kMaxNumberChars = 330;
+char* put_f(char* o, double v) {
+    uint64_t bits;
+    std::memcpy(&bits, &v, sizeof(bits));
+    const int be = (int)((bits >> 52) & 0x7ff);
+    const int e = (be ? be : 1) - 1075;
+    if (be == 0x7ff || std::fabs(v) >= 9.0e12 || e >= 0) {
+        const auto res = std::to_chars(o, o + kMaxNumberChars, v, std::chars_format::fixed, 6);
+        if (res.ec == std::errc()) return res.ptr;
+        const int n = std::snprintf(o, kMaxNumberChars, "%f", v);
+        return o + (n > 0 ? std::min<size_t>((size_t)n, kMaxNumberChars - 1) : 0);
     }
+    const uint64_t m = (bits & ((uint64_t(1) << 52) - 1)) | (be ? uint64_t(1) << 52 : 0);
+    const int s = -e;  // m * 10^6 < 2^73: from s = 74 on, q = 0 and the remainder is below one half
+    uint64_t q = 0;
+    if (s < 74) {
+        const unsigned __int128 num = (unsigned __int128)m * 1000000u;
+        unsigned __int128 qq = num >> s;
+        const unsigned __int128 rem = num - (qq << s);
+        const unsigned __int128 half = (unsigned __int128)1 << (s - 1);
+        if (rem > half || (rem == half && (qq & 1))) qq++;
+        q = (uint64_t)qq;
+    }
+    if (bits >> 63) *o++ = '-';
+    uint64_t ip = q / 1000000, fp = q % 1000000;
+    char t[24];
+    int k = 0;
+    do {
+        t[k++] = (char)('0' + ip % 10);
+        ip /= 10;
+    } while (ip);
+    while (k) *o++ = t[--k];
+    *o++ = '.';
+    for (int d = 5; d >= 0; d--) {
+        o[d] = (char)('0' + fp % 10);
+        fp /= 10;
+    }
+    return o + 6;
 }
 
 }  // namespace
@@ -143,26 +181,47 @@ extern "C" int rrsph_layer_write(const char* csv_path, const rrsph_params* p, co
     if (wp) head += ",p";
     head += '\n';
     // the lines of particles [i0, i1) into out
+    const size_t max_line = 8 * (kMaxNumberChars + 1) + 32;
     auto lines = [&](uint64_t i0, uint64_t i1, std::string& out) {
-        out.reserve((size_t)(i1 - i0) * 96);
-        char ibuf[32];
+        out.resize((size_t)(i1 - i0) * 64 + max_line);
+        size_t used = 0;
         for (uint64_t i = i0; i < i1; i++) {
+            if (out.size() - used < max_line) out.resize(2 * out.size());
+            char* const b = &out[0] + used;
+            char* o = b;
             const double* ri = r + i * stride;
-            put_f(out, ri[0]); out += ',';
-            put_f(out, ri[1]); out += ',';
-            if (d3) { put_f(out, ri[2]); out += ','; }
-            const auto res = std::to_chars(ibuf, ibuf + sizeof(ibuf), (long)itype[i]);
-            out.append(ibuf, (size_t)(res.ptr - ibuf));
+            o = put_f(o, ri[0]);
+            *o++ = ',';
+            o = put_f(o, ri[1]);
+            *o++ = ',';
+            if (d3) {
+                o = put_f(o, ri[2]);
+                *o++ = ',';
+            }
+            o = std::to_chars(o, o + 16, (long)itype[i]).ptr;
             if (wv) {
                 const double* vi = v + i * stride;
-                out += ','; put_f(out, vi[0]);
-                out += ','; put_f(out, vi[1]);
-                if (d3) { out += ','; put_f(out, vi[2]); }
+                *o++ = ',';
+                o = put_f(o, vi[0]);
+                *o++ = ',';
+                o = put_f(o, vi[1]);
+                if (d3) {
+                    *o++ = ',';
+                    o = put_f(o, vi[2]);
+                }
             }
-            if (wr) { out += ','; put_f(out, rho[i]); }
-            if (wp) { out += ','; put_f(out, pres[i]); }
-            out += '\n';
+            if (wr) {
+                *o++ = ',';
+                o = put_f(o, rho[i]);
+            }
+            if (wp) {
+                *o++ = ',';
+                o = put_f(o, pres[i]);
+            }
+            *o++ = '\n';
+            used += (size_t)(o - b);
         }
+        out.resize(used);
     };
     // contiguous ranges formatted in parallel, written in order (the same bytes)
     const uint64_t n = p->ntotal;

@@ -197,12 +197,21 @@ def test_layer_numbers_format_like_printf(tmp_path):
     """Layer values must print exactly as std::to_string (printf "%f")."""
     from sph2d_gb300 import cases, write_layer
 
-    case = cases.dam_break_2d(nx=10, ny=10)
+    case = cases.dam_break_2d(nx=60, ny=60)
     p = case.params()
     n = case.ntotal
     rng = np.random.default_rng(3)
-    specials = np.array([0.0078125, -0.0078125, 2.5e-7, 0.5e-6, 123456789.123456789, -1e-9, 1e15 + 0.5, 0.1, 0.3])
-    vals = np.concatenate([specials, rng.normal(0, 10, n - len(specials)) * 10.0 ** rng.integers(-8, 8, n - len(specials))])
+    specials = np.array([0.0078125, -0.0078125, 2.5e-7, 0.5e-6, 123456789.123456789, -1e-9, 1e15 + 0.5, 0.1, 0.3,
+                         -0.0, 0.0, 0.9999995, 0.99999949999, 8.999999999999e12, 9.0e12, -9.0e12, 1e300, -1e-310,
+                         5e-324, 2.0 ** -74, 4.5e15, np.inf, -np.inf])
+    m = n - len(specials)
+    # ties in millionths: odd multiples of 2^-7; random bit patterns over the exponents of
+    # |v| in [2^-40, 2^50); plain normals over ten decades
+    ties = (2 * rng.integers(0, 2**40, m // 3) + 1) / 128.0 * rng.choice([-1, 1], m // 3)
+    bits = (rng.integers(0, 2**52, m // 3, dtype=np.int64) | (rng.integers(1023 - 40, 1023 + 50, m // 3) << 52))
+    pats = bits.view(np.float64) * rng.choice([-1, 1], m // 3)
+    rest = rng.normal(0, 10, m - 2 * (m // 3)) * 10.0 ** rng.integers(-8, 8, m - 2 * (m // 3))
+    vals = np.concatenate([specials, ties, pats, rest])
     r = np.stack([vals, -vals[::-1]], axis=1)
     write_layer(tmp_path / "x.csv", p, r, r, vals, vals, case.itype, dump=True)
     lines = (tmp_path / "x.csv").read_text().splitlines()[1:]
