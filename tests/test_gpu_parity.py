@@ -776,3 +776,55 @@ def test_neighbour_reuse_with_delta_sph(gpu_available, dim):
     assert pa == pb
     for k in ("r", "v", "rho"):
         assert rel_l2(a[k], b[k]) < 1e-5, (k, rel_l2(a[k], b[k]))
+
+
+@pytest.mark.parametrize("dim,max_nb", [(2, 64), (2, 100), (3, 256), (3, 400)])
+def test_neighbour_reuse_with_over_full_candidate_lists(gpu_available, dim, max_nb):
+    """Particles with more candidates than a list holds (64 in 2D, 256 in 3D;
+    here h = 2.0 dx in 2D and 1.75 dx in 3D, a few hundred such particles,
+    over five steps: the lattice laid out for h = 1.4 dx resp. 1.3 dx
+    compresses under the longer h, and the oracle finds 56 resp. 251
+    neighbours at most by then, more a few steps later) are searched by
+    stencil every step and the grid is rebuilt every step while one exists: the pair counts equal the per-step search's, the state
+    stays within float rounding of it, and graph replay equals direct launches
+    bit for bit. max_neighbours at most the capacity + 1 fuses the whole step
+    into the force gather (which then reads the neighbours the density pass
+    wrote for the over-full lists); above it the force gather searches the
+    stencil itself."""
+    from sph2d_gb300 import Solver, cases
+
+    if dim == 2:
+        case = _dam(nx=40, ny=20)
+        case.model["intf_hsml_coef"] = 2.0
+    else:
+        case = cases.dam_break_3d(dx=0.02, block=(0.3, 0.3, 0.3), density_treatment=0)
+        case.model["intf_hsml_coef"] = 1.75
+    case.model["max_neighbours"] = max_nb
+    p = case.params()
+    assert p.max_neighbours == max_nb
+    steps = 5
+    out = []
+    for reuse in (True, False):
+        with Solver(p, "mixed") as s:
+            s.set_neighbour_reuse(reuse)
+            s.upload(case.r, case.v, case.rho, case.itype)
+            pairs = []
+            t = 0.0
+            for _ in range(steps):
+                t = s.step(1, t)
+                pairs.append(s.pair_count()[0])
+            out.append((s.download(), pairs, s.neighbour_rebuilds()))
+    (a, pa, ra), (b, pb, rb) = out
+    assert pa == pb
+    assert rb == 0 and ra == steps  # an over-full list asks for a fresh grid every step
+    for k in ("r", "v", "rho"):
+        assert rel_l2(a[k], b[k]) < 1e-5, (k, rel_l2(a[k], b[k]))
+    runs = []
+    for timing in (False, True):
+        with Solver(p, "mixed") as s:
+            s.set_phase_timing(timing)
+            s.upload(case.r, case.v, case.rho, case.itype)
+            s.step(steps, 0.0)
+            runs.append(s.download())
+    for k in ("r", "v", "rho", "p"):
+        assert np.array_equal(runs[0][k], runs[1][k]), k
