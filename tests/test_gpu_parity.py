@@ -828,3 +828,71 @@ def test_neighbour_reuse_with_over_full_candidate_lists(gpu_available, dim, max_
             runs.append(s.download())
     for k in ("r", "v", "rho", "p"):
         assert np.array_equal(runs[0][k], runs[1][k]), k
+
+
+@pytest.mark.parametrize("what", ["non_existent", "consistency_fix"])
+def test_mixed_step_skips_non_existent_particles(gpu_available, what):
+    """The FP32-mixed step with particles that do not exist: every seventh one
+    from the start, or one that leaves the geometry in the first step and is
+    made non-existent (CONSISTENCY_FIX) while the candidate lists of its
+    neighbours still hold it. Against the oracle (float rounding) and against
+    the same step searching every step (the same pairs every step)."""
+    from oracle import binding as O
+    from sph2d_gb300 import Solver
+
+    case = _dam(nx=40, ny=20)
+    p = case.params()
+    itype, v = case.itype.copy(), case.v.copy()
+    if what == "non_existent":
+        itype[::7] = 0
+    else:
+        v[0] = [0.0, -1.0e4]  # leaves the geometry box in one step
+        p.consistency_treatment = 2
+    steps = 5
+    ref = O.run(p, case.r, v, case.rho, itype, nsteps=steps)
+    out = []
+    for reuse in (True, False):
+        with Solver(p, "mixed") as s:
+            s.set_neighbour_reuse(reuse)
+            s.upload(case.r, v, case.rho, itype)
+            pairs = []
+            t = 0.0
+            for _ in range(steps):
+                t = s.step(1, t)
+                pairs.append(s.pair_count()[0])
+            out.append((s.download(), pairs))
+    (a, pa), (b, pb) = out
+    assert pa == pb
+    assert np.array_equal(a["itype"], ref["itype"])
+    if what == "consistency_fix":
+        assert a["itype"][0] == 0
+    live = ref["itype"] != 0
+    for st in (a, b):
+        assert rel_l2(st["r"][live], ref["r"][live]) < 1e-8
+        assert rel_l2(st["v"][live], ref["v"][live]) < 1e-4
+        assert rel_l2(st["rho"][live], ref["rho"][live]) < 1e-6
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 2047, 2049])
+def test_mixed_step_at_ragged_and_tiny_particle_counts(gpu_available, n):
+    """The FP32-mixed step (candidate-list reuse) at counts that are not a
+    multiple of any block or list group, including one particle, against the
+    oracle."""
+    from oracle import binding as O
+    from sph2d_gb300 import Solver, derive, params_from_json
+
+    base = _dam(nx=60, ny=40)
+    idx = np.random.default_rng(n).choice(base.ntotal, size=n, replace=False)
+    idx.sort()
+    particle = dict(base.particle, ntotal=n, nfluid=int(np.sum(idx < base.particle["nfluid"])),
+                    nvirt=int(np.sum(idx >= base.particle["nfluid"])))
+    r, v, rho, it = base.r[idx], base.v[idx], base.rho[idx], base.itype[idx]
+    p = derive(params_from_json(base.model, particle), r)
+    ref = O.run(p, r, v, rho, it, nsteps=4)
+    with Solver(p, "mixed") as s:
+        s.upload(r, v, rho, it)
+        s.step(4, 0.0)
+        st = s.download()
+    assert rel_l2(st["r"], ref["r"]) < 1e-8
+    assert rel_l2(st["v"], ref["v"]) < 1e-4
+    assert rel_l2(st["rho"], ref["rho"]) < 1e-6
