@@ -3,7 +3,7 @@
 Two checkers live here:
 
 - the C restatement of RRSPH_OMP's step in ``oracle/rrsph_oracle.c``
-  (``oracle/liboracle.so``), usable wherever gcc is (including the GPU box);
+  (``oracle/liboracle.so``), usable wherever gcc is;
 - the reference's own OMP compute core compiled from its sources by
   ``oracle/build_ref.sh`` (``oracle/_ref/rrsph_ref``), driven through files,
   available only where the reference sources were present at build time.

@@ -3,8 +3,8 @@
 Runs the reference's RRSPH_OMP compute core (built from its sources into
 oracle/_ref/rrsph_ref by oracle/build_ref.sh) on seeded synthetic cases from
 sph2d_gb300.cases and stores its outputs, so that machines without the
-reference sources (the GPU machine) can still pin the oracle and the CUDA path to
-the reference's results.
+reference sources can still pin the oracle and the CUDA path to the
+reference's results.
 
 Cases (small versions of the benchmark workloads, to keep the file small):
   dam: dam_break_2d(nx=50, ny=25, seed=1), continuity density
