@@ -124,3 +124,33 @@ def test_consistency_stop_writes_a_crash_dump(gpu_available, tmp_path):
     crash = list(tmp_path.glob("crash_dump_*.csv"))
     assert len(crash) == 1
     assert crash[0].read_text().splitlines()[0] == "x,y,itype,vx,vy,rho,p"
+
+
+def test_run_3d_layers_match_the_oracle(gpu_available, tmp_path):
+    """rrsph_run of a 3D case (FP32-mixed step, neighbour reuse): the data
+    layer names, the 3D columns, and the last layer against the oracle run
+    for the same steps (mixed-precision tolerance)."""
+    from oracle import binding as O
+    from sph2d_gb300 import Solver, cases, read_layer
+
+    case = cases.dam_break_3d(dx=0.02, block=(0.3, 0.3, 0.3), density_treatment=0)
+    dt = case.model["dt"]
+    case.model.update({"simulation_time": 12 * dt, "save_time": 5 * dt, "use_dump": False})
+    case.write_experiment(tmp_path)
+    p = case.params()
+    with Solver(p, "mixed") as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        t, n = s.run(tmp_path, 0.0)
+    saves, _, steps, save_steps = _expected_layers(0.0, p.dt, p.simulation_time, p.save_time, p.dump_time, False)
+    assert n == steps
+    sd = _digits(p.save_time)
+    data = sorted((tmp_path / "data").iterdir(), key=lambda f: float(f.stem))
+    assert [f.name for f in data] == [f"{t:.{sd}f}.csv" for t in saves]
+    assert data[-1].read_text().splitlines()[0].startswith("x,y,z,itype,vx,vy,vz")
+    ref = O.run(p, case.r, case.v, case.rho, case.itype, nsteps=save_steps[-1])
+    r, v, rho, pres, itype = read_layer(data[-1], p)
+    # the layer prints six decimals; the mixed step adds float rounding
+    assert np.array_equal(itype, ref["itype"])
+    assert np.allclose(r, ref["r"], rtol=0.0, atol=1e-6)
+    assert rel_l2(v, ref["v"]) < 1e-4
+    assert rel_l2(rho, ref["rho"]) < 1e-6
