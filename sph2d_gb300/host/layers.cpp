@@ -34,6 +34,16 @@ namespace {
 // fixed format and precision 6, which is specified to match printf.
 // Writes at most kMaxNumberChars characters at o; returns the end.
 constexpr size_t kMaxNumberChars = 330;
+struct Digits2 {  // "00", "01", ..., "99"
+    char d[200];
+    constexpr Digits2() : d() {
+        for (int i = 0; i < 100; i++) {
+            d[2 * i] = (char)('0' + i / 10);
+            d[2 * i + 1] = (char)('0' + i % 10);
+        }
+    }
+};
+constexpr Digits2 kDigits2{};
 char* put_f(char* o, double v) {
     uint64_t bits;
     std::memcpy(&bits, &v, sizeof(bits));
@@ -57,19 +67,28 @@ char* put_f(char* o, double v) {
         q = (uint64_t)qq;
     }
     if (bits >> 63) *o++ = '-';
-    uint64_t ip = q / 1000000, fp = q % 1000000;
-    char t[24];
-    int k = 0;
-    do {
-        t[k++] = (char)('0' + ip % 10);
-        ip /= 10;
-    } while (ip);
-    while (k) *o++ = t[--k];
-    *o++ = '.';
-    for (int d = 5; d >= 0; d--) {
-        o[d] = (char)('0' + fp % 10);
-        fp /= 10;
+    uint64_t ip = q / 1000000;  // < 9e12: at most 13 digits
+    const uint32_t fp = (uint32_t)(q % 1000000);
+    // the integer part, two digits at a time from the right
+    char t[16];
+    int k = 16;
+    while (ip >= 100) {
+        k -= 2;
+        std::memcpy(t + k, kDigits2.d + 2 * (ip % 100), 2);
+        ip /= 100;
     }
+    if (ip >= 10) {
+        k -= 2;
+        std::memcpy(t + k, kDigits2.d + 2 * ip, 2);
+    } else {
+        t[--k] = (char)('0' + ip);
+    }
+    std::memcpy(o, t + k, (size_t)(16 - k));
+    o += 16 - k;
+    *o++ = '.';
+    std::memcpy(o, kDigits2.d + 2 * (fp / 10000), 2);
+    std::memcpy(o + 2, kDigits2.d + 2 * (fp / 100 % 100), 2);
+    std::memcpy(o + 4, kDigits2.d + 2 * (fp % 100), 2);
     return o + 6;
 }
 
@@ -237,7 +256,7 @@ extern "C" int rrsph_layer_write(const char* csv_path, const rrsph_params* p, co
     if (!f) return set_error(RRSPH_ERR_IO, std::string("cannot write layer ") + csv_path);
     bool ok = std::fwrite(head.data(), 1, head.size(), f) == head.size();
     for (const auto& c : chunk) ok = ok && std::fwrite(c.data(), 1, c.size(), f) == c.size();
-    std::fclose(f);
+    ok = (std::fclose(f) == 0) && ok;
     if (!ok) return set_error(RRSPH_ERR_IO, std::string("short write of layer ") + csv_path);
     return RRSPH_OK;
 }
