@@ -219,3 +219,16 @@ def test_layer_numbers_format_like_printf(tmp_path):
         f = line.split(",")
         assert f[0] == "%f" % r[i, 0] and f[1] == "%f" % r[i, 1], (i, f[:2], r[i])
         assert f[5] == "%f" % vals[i]
+
+
+def test_empty_particle_set_is_an_error():
+    """No particles: the derivations refuse the counts (the solver would have
+    nothing to step), and so do counts with more fluid than particles."""
+    from sph2d_gb300 import RrsphError, derive, params_from_json
+
+    p = params_from_json(_model(), _particle(ntotal=0, nfluid=0, nvirt=0))
+    with pytest.raises(RrsphError, match="bad particle counts"):
+        derive(p, np.zeros((0, 2)))
+    q = params_from_json(_model(), _particle(ntotal=10, nfluid=11, nvirt=0))
+    with pytest.raises(RrsphError, match="bad particle counts"):
+        derive(q, np.zeros((10, 2)))
