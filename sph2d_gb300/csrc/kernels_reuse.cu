@@ -326,8 +326,9 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
 
 // update_acceleration over this step's neighbours: the list the density pass
 // wrote (or the stencil search for an overflowed list). In 2D a neighbour's
-// pressure comes with its velocity and density (V4.z); in 3D from PR. STD (2D):
-// the common method set of ForceAcc::pair_std, fixed at compile time. At most
+// pressure comes with its velocity and density (V4.z); in 3D from PR. STD: the
+// common method set of ForceAcc::pair_std (2D) / pair_std3 (3D), fixed at
+// compile time. At most
 // 64 registers (4 blocks of 256 threads per SM): the gather hides its L1/L2
 // latency with warps.
 // WV != 0: the whole step follows in the same thread (whole_particle with
@@ -404,6 +405,8 @@ __global__ void __launch_bounds__(kMaxGatherThreads, 4) k_forces_verlet(DevParam
                             F.cax = F.cay = F.caz = F.cvx = F.cvy = F.cvz = 0.0f;
                             if (DIM == 2 && STD) {
                                 F.pair_std(vb[j], dx, dy, d2, __float_as_int(pb[j].w));
+                            } else if (DIM == 3 && STD) {
+                                F.pair_std3(vb[j], rb[j], dx, dy, dz, d2, __float_as_int(pb[j].w));
                             } else {
                                 float2 pri;
                                 if (DIM == 3) {
@@ -536,8 +539,7 @@ template <int DIM>
 void launch_forces_verlet(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal,
                           StepScalars* scal_next, uint32_t* flags, cudaStream_t st, int threads, int whole) {
     const unsigned blocks = (P.n + threads - 1) / threads;
-    const bool std_terms = DIM == 2 && P.all_cubic && P.intf_form != 1 && P.art_visc && !P.art_pressure &&
-                           !P.avg_vel;
+    const bool std_terms = P.all_cubic && P.intf_form != 1 && P.art_visc && !P.art_pressure && !P.avg_vel;
     const int wv = whole ? (kVarMixed | (P.density_treatment != 0 ? kVarCont : 0) |
                             (P.avg_vel || P.dt_method == 2 ? kVarRare : 0))
                          : 0;
@@ -555,9 +557,7 @@ void launch_forces_verlet(const DevParams& P, const State& S, const Sorted& G, S
         default: RRSPH_FV(SKF, STD, kVarMixed | kVarCont | kVarRare);                  \
         }                                                                              \
     } while (0)
-    // STD = DIM == 2: the common-method variant exists in 2D only (std_terms is
-    // false in 3D), so no 3D instance of it is compiled
-    if (DIM == 2 && std_terms) RRSPH_FV_WV(1, (DIM == 2));
+    if (std_terms) RRSPH_FV_WV(1, true);
     else if (P.all_cubic) RRSPH_FV_WV(1, false);
     else RRSPH_FV_WV(0, false);
 #undef RRSPH_FV_WV

@@ -197,6 +197,28 @@ struct ForceAcc {
         cax += dx * m;
         cay += dy * m;
     }
+    // pair_with for the common method set, 3D (the same switches as pair_std);
+    // the neighbour's p/rho^2 comes from its pressure pair (pri.y).
+    __device__ __forceinline__ void pair_std3(const float4 vi, const float2 pri, float dx, float dy, float dz,
+                                              float d2, int32_t ti) {
+        const MixedF& M = P.mf;
+        const float inv_dist = rsqrtf(d2);
+        const float dist = d2 * inv_dist;
+        const float q = dist * M.inv_h;
+        float m = 0.0f;
+        if (ext && ti < 0 && dist < M.lj_rr0) m -= lj_coef(M, inv_dist);
+        const float rhoi = vi.w;
+        const float sc = kernel_dwdr_scalef(1, M.kf[1], q, inv_dist, M.inv_h);
+        m += sc * (pri.y + prj.y) * M.mass;
+        const float vr = -((vj.x - vi.x) * dx + (vj.y - vi.y) * dy + (vj.z - vi.z) * dz);
+        const float mu = fminf(__fdividef(M.h * vr, d2 + M.etq_h2), 0.0f);
+        arvmu = fmaxf(arvmu, -mu);
+        const float piv = __fdividef((M.av_beta * mu - M.av_alpha_c) * mu, 0.5f * (rhoi + rhoj));
+        m += sc * piv * M.mass;
+        cax += dx * m;
+        cay += dy * m;
+        caz += dz * m;
+    }
 };
 
 }  // namespace
