@@ -183,7 +183,8 @@ __device__ __forceinline__ float density_term(const MixedF& M, int skf, float f,
     const float inv_dist = rsqrtf(d2);
     const float q = d2 * inv_dist * M.inv_h;
     if (!CONT) return SKF == 1 ? cubic_wf_sel(f, q) : kernel_wf(skf, f, q);
-    const float sc = kernel_dwdr_scalef(skf, f, q, inv_dist, M.inv_h);
+    const float sc = SKF == 1 ? cubic_dwdr_sel(f, q, inv_dist, M.inv_h)
+                              : kernel_dwdr_scalef(skf, f, q, inv_dist, M.inv_h);
     const float vcc = (vdi.x - vdj.x) * dx + (vdi.y - vdj.y) * dy + (vdi.z - vdj.z) * dz;
     float term = vcc * sc;
     if (delta) {

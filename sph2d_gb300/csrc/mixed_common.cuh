@@ -208,7 +208,7 @@ struct ForceAcc {
         float m = 0.0f;
         if (ext && ti < 0 && dist < M.lj_rr0) m -= lj_coef(M, inv_dist);
         const float rhoi = vi.w;
-        const float sc = kernel_dwdr_scalef(1, M.kf[1], q, inv_dist, M.inv_h);
+        const float sc = cubic_dwdr_sel(M.kf[1], q, inv_dist, M.inv_h);
         m += sc * (pri.y + prj.y) * M.mass;
         const float vr = -((vj.x - vi.x) * dx + (vj.y - vi.y) * dy + (vj.z - vi.z) * dz);
         const float mu = fminf(__fdividef(M.h * vr, d2 + M.etq_h2), 0.0f);
