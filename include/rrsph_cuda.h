@@ -261,6 +261,11 @@ typedef struct rrsph_diagnostics {
     uint64_t boundary;     /* boundary particles */
 } rrsph_diagnostics;
 int rrsph_diagnostics_get(rrsph_solver* s, rrsph_diagnostics* out);
+/* The rates of the last completed step: the accelerations a (the a_var that
+ * update_acceleration wrote, UpdateAcceleration.cpp:33-125, stride `stride`)
+ * and, with continuity density, drho (density_con, Density.h:63-114). Either
+ * may be NULL. Zero after an upload, as the loop's fresh work arrays. */
+int rrsph_download_rates(rrsph_solver* s, double* a, uint32_t stride, double* drho);
 /* Directed neighbour pairs (the entries find_neighbours would list) of the
  * last completed step, and summed over the steps since rrsph_upload. */
 int rrsph_pair_count(rrsph_solver* s, uint64_t* last_step, uint64_t* total);
@@ -280,6 +285,18 @@ int rrsph_grid_find(rrsph_solver* s, uint32_t* keys, uint32_t* grid,
  * counts[j] <= max_per; otherwise RRSPH_ERR_NEIGHBOUR_OVERFLOW. */
 int rrsph_neighbours(rrsph_solver* s, uint32_t* counts, uint32_t* list,
                      uint32_t max_per, uint64_t* total_pairs);
+/* The neighbour pairs the last completed step of the FP32-mixed solver with
+ * neighbour reuse used: the list its density pass wrote (the candidates that
+ * passed the reference's cutoff test of find_neighbours, GridFind.cpp:124,
+ * 150-156, in float with a double re-test near the cutoff, or the stencil
+ * search of a particle whose candidate list overflowed), as particle ids:
+ * counts[j], list[j*max_per + n]. The order within a row is the candidate
+ * order of the last list build, not the reference's; the sets are the
+ * reference's. RRSPH_ERR_UNSUPPORTED for other solvers; RRSPH_ERR_INVALID_ARGUMENT
+ * when no step has run since the last upload, loop-piece call or reuse
+ * setting; RRSPH_ERR_NEIGHBOUR_OVERFLOW when a row does not fit max_per. */
+int rrsph_step_neighbours(rrsph_solver* s, uint32_t* counts, uint32_t* list,
+                          uint32_t max_per, uint64_t* total_pairs);
 /* density_sum (Density.h:25-61) or density_con (Density.h:63-114) by
  * density_treatment, on r, v, rho of the uploaded state. Writes rho (summation)
  * or drho (continuity) into out_rho_or_drho and p into out_p, and stores rho/p
@@ -300,15 +317,19 @@ int rrsph_forces(rrsph_solver* s, uint32_t terms, double* a, uint32_t stride,
  * allocate device memory (code whose device memory belongs to another
  * framework's pool, or a step loop that must not allocate because cudaMalloc
  * can block or fail mid-run). No counterpart in the reference.
- * Every pointer is a device pointer owned by the caller; outputs must not
- * overlap inputs, and the inputs are left unchanged. The working memory is a
+ * Every pointer is a device pointer owned by the caller; the two outputs must
+ * not overlap the inputs or each other (any overlap of the n-word ranges is
+ * refused with RRSPH_ERR_INVALID_ARGUMENT), and the inputs are left unchanged.
+ * A CUDA error already pending from the caller's earlier work is returned as
+ * RRSPH_ERR_CUDA and left pending. The working memory is a
  * fixed array inside the library (about 9.4 MB; every GPU that loads the
  * library holds it until the process exits), so n is limited to
  * RRSPH_SORT_NOALLOC_MAX_PAIRS and a larger n returns
  * RRSPH_ERR_INVALID_ARGUMENT. The call allocates nothing and is asynchronous
  * on `stream` (a cudaStream_t; NULL = the default stream). Its first call on a
- * device looks up the array's device address; make that first call before any
- * stream capture. All calls on a device share the array, so calls that may
+ * device looks up the array's device address and keeps it for the process;
+ * make that first call before any stream capture, and do not call it on a
+ * device after a cudaDeviceReset of that device. All calls on a device share the array, so calls that may
  * overlap on the GPU race: order them (one stream, or events). */
 int rrsph_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* ids_in,
                              uint32_t* keys_out, uint32_t* ids_out, uint32_t n,

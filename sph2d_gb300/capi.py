@@ -182,6 +182,8 @@ _SIGS = {
     "rrsph_pair_count": (C.c_int, [C.c_void_p, _P(C.c_uint64), _P(C.c_uint64)]),
     "rrsph_grid_find": (C.c_int, [C.c_void_p, _u32p, _u32p, _u32p]),
     "rrsph_neighbours": (C.c_int, [C.c_void_p, _u32p, _u32p, C.c_uint32, _P(C.c_uint64)]),
+    "rrsph_step_neighbours": (C.c_int, [C.c_void_p, _u32p, _u32p, C.c_uint32, _P(C.c_uint64)]),
+    "rrsph_download_rates": (C.c_int, [C.c_void_p, _dp, C.c_uint32, _dp]),
     "rrsph_density": (C.c_int, [C.c_void_p, _dp, _dp]),
     "rrsph_forces": (C.c_int, [C.c_void_p, C.c_uint32, _dp, C.c_uint32, _dp, _dp]),
     "rrsph_phase_count": (C.c_int, [C.c_void_p, _P(C.c_int)]),

@@ -155,6 +155,22 @@ __device__ __forceinline__ double f2d(float f) {
     return (double)f;
 }
 
+// The float copy of (v, rho - rho0) that density_con reads of a neighbour. In
+// 2D the unused z carries the low part of rho - rho0 (the double minus its
+// float), so that rho_i - rho_j keeps ~1e-7 of the difference itself: the
+// deviations are ~5 at half a metre of water and differ by ~0.1 between
+// neighbours, so one float each would leave ~3e-6 of the difference.
+template <int DIM>
+__device__ __forceinline__ float4 vd4_of(double vx, double vy, double vz, double drho0) {
+    const float hi = d2f(drho0);
+    return make_float4(d2f(vx), d2f(vy), DIM == 3 ? d2f(vz) : d2f(drho0 - f2d(hi)), hi);
+}
+// rho_i - rho_j from two such copies.
+template <int DIM>
+__device__ __forceinline__ float vd4_drho(float4 vdi, float4 vdj) {
+    return DIM == 3 ? vdi.w - vdj.w : (vdi.w - vdj.w) + (vdi.z - vdj.z);
+}
+
 // ---------------------------------------------------------------- Morton --
 // GridUtils.h:50-64 and 92-104, computed in 64-bit like rr_uint.
 __host__ __device__ inline uint64_t split2(uint64_t x) {

@@ -124,6 +124,11 @@ void launch_verlet_reset(uint32_t* rebuild, uint32_t* gone, unsigned long long* 
 void launch_verlet_upload_check(uint32_t* rebuild, const uint32_t* gone, cudaStream_t st);
 template <int DIM>
 void launch_verlet_build(const DevParams& P, const State& S, const Sorted& G, cudaStream_t st);
+// The last reuse step's neighbour list (nlist / ncount) as particle ids:
+// counts[id], list[id * max_per + e]; more than max_per raises the overflow flag.
+template <int DIM>
+void launch_nlist_export(const DevParams& P, const Sorted& G, uint32_t* counts, uint32_t* list, uint32_t max_per,
+                         uint32_t* flags, cudaStream_t st);
 template <int DIM>
 void launch_density_verlet(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
                            cudaStream_t st, int threads);

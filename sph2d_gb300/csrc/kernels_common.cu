@@ -96,8 +96,7 @@ __global__ void k_reorder(DevParams P, State S, Sorted G, GatherSrc F) {
     }
     G.V4[k] = make_float4(fvx, fvy, fvz, frho);
     if (R == 2 || (R == 3 && P.density_treatment != 0))  // rho - rho0 keeps rho_i - rho_j accurate in float
-        G.VD4[k] = make_float4(d2f(S.vx[id]), d2f(S.vy[id]), DIM == 3 ? d2f(S.vz[id]) : 0.0f,
-                               d2f(S.rho[id] - P.rho0));
+        G.VD4[k] = vd4_of<DIM>(S.vx[id], S.vy[id], DIM == 3 ? S.vz[id] : 0.0, S.rho[id] - P.rho0);
 }
 
 // make_waves (WaveMaker.cpp:4-32, piston call enabled) + whole_step

@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_mixed(DevParams P
                         if (delta) {
                             // r_factor = dot(r_j - r_i, diff * sc) / |diff|^2 = -sc;
                             // rho_factor = (rho_i - rho_j) / rho_i on the deviations from rho0
-                            const float rho_factor = __fdividef(vdi.w - vdj.w, M.rho0 + vdi.w);
+                            const float rho_factor = __fdividef(vd4_drho<DIM>(vdi, vdj), M.rho0 + vdi.w);
                             term += 2.0f * M.dhc * (rho_factor * -sc);
                         }
                         part += term;

@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_vl_build(DevParams P, Sta
 // One candidate's contribution to the density gather: W (summation) or the
 // continuity rate with its delta-SPH term (density_con, Density.h:63-114,
 // the same arithmetic as k_density_mixed).
-template <int SKF, bool CONT>
+template <int DIM, int SKF, bool CONT>
 __device__ __forceinline__ float density_term(const MixedF& M, int skf, float f, float dx, float dy, float dz,
                                               float d2, float4 vdi, float4 vdj, bool delta) {
     const float inv_dist = rsqrtf(d2);
@@ -185,10 +185,11 @@ __device__ __forceinline__ float density_term(const MixedF& M, int skf, float f,
     if (!CONT) return SKF == 1 ? cubic_wf_sel(f, q) : kernel_wf(skf, f, q);
     const float sc = SKF == 1 ? cubic_dwdr_sel(f, q, inv_dist, M.inv_h)
                               : kernel_dwdr_scalef(skf, f, q, inv_dist, M.inv_h);
-    const float vcc = (vdi.x - vdj.x) * dx + (vdi.y - vdj.y) * dy + (vdi.z - vdj.z) * dz;
+    float vcc = (vdi.x - vdj.x) * dx + (vdi.y - vdj.y) * dy;
+    if (DIM == 3) vcc += (vdi.z - vdj.z) * dz;
     float term = vcc * sc;
     if (delta) {
-        const float rho_factor = __fdividef(vdi.w - vdj.w, M.rho0 + vdi.w);
+        const float rho_factor = __fdividef(vd4_drho<DIM>(vdi, vdj), M.rho0 + vdi.w);
         term += 2.0f * M.dhc * (rho_factor * -sc);
     }
     return term;
@@ -253,7 +254,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
                                   d2 < M.cut2_hi;
                         if (in && !(d2 < M.cut2_lo)) in = within_cutoff<DIM>(P, S, G, en[j] & IDX, k, d2);
                         const float4 vdi = CONT && in ? G.VD4[en[j] & IDX] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                        const float t = density_term<SKF, CONT>(M, skf, f, dx, dy, dz, d2, vdi, vdj, delta);
+                        const float t = density_term<DIM, SKF, CONT>(M, skf, f, dx, dy, dz, d2, vdi, vdj, delta);
                         part += in ? t : 0.0f;
                         if (in) nslab[(size_t)(cnt >> 2) * 4 * P.n + (cnt & 3u)] = en[j];
                         cnt += in;
@@ -289,7 +290,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
                             nslab[(size_t)(cnt >> 2) * 4 * P.n + (cnt & 3u)] = i | vl_code<DIM>(sx, sy, sz);
                         cnt++;
                         const float4 vdi = CONT ? G.VD4[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                        part += density_term<SKF, CONT>(M, skf, f, dx, dy, dz, d2, vdi, vdj, delta);
+                        part += density_term<DIM, SKF, CONT>(M, skf, f, dx, dy, dz, d2, vdi, vdj, delta);
                     }
                     acc.add(M.mass * part);
                 }
@@ -564,6 +565,42 @@ void launch_forces_verlet(const DevParams& P, const State& S, const Sorted& G, S
 #undef RRSPH_FV_WV
 #undef RRSPH_FV
 }
+
+namespace {
+
+// The neighbour list the last density pass of the reuse step wrote (nlist,
+// ncount: build slots with cell codes, in list order), as particle ids: row
+// G.id[k] of `list` gets the ids of slot k's entries.
+template <int DIM>
+__global__ void k_nlist_export(DevParams P, Sorted G, uint32_t* __restrict__ counts, uint32_t* __restrict__ list,
+                               uint32_t max_per, uint32_t* __restrict__ flags) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= P.n) return;
+    const uint32_t id = G.id[k], c = G.ncount[k];
+    counts[id] = c;
+    // a searched (over-full) particle stores at most the list capacity: a full
+    // row may have lost entries, which this copy cannot show
+    const bool clipped = c == (uint32_t)Vl<DIM>::cap && G.vcount[k] == kListOver;
+    if (c > max_per || clipped) atomicOr(flags, RRSPH_FLAG_NEIGHBOUR_OVERFLOW);
+    const uint32_t* const nslab = G.nlist + (size_t)k * 4;
+    const uint32_t m = c < max_per ? c : max_per;
+    for (uint32_t e = 0; e < m; e++)
+        list[(size_t)id * max_per + e] = G.id[nslab[(size_t)(e >> 2) * 4 * P.n + (e & 3u)] & Vl<DIM>::index];
+}
+
+}  // namespace
+
+template <int DIM>
+void launch_nlist_export(const DevParams& P, const Sorted& G, uint32_t* counts, uint32_t* list, uint32_t max_per,
+                         uint32_t* flags, cudaStream_t st) {
+    const unsigned blocks = (P.n + 255) / 256;
+    k_nlist_export<DIM><<<blocks, 256, 0, st>>>(P, G, counts, list, max_per, flags);
+}
+
+template void launch_nlist_export<2>(const DevParams&, const Sorted&, uint32_t*, uint32_t*, uint32_t, uint32_t*,
+                                     cudaStream_t);
+template void launch_nlist_export<3>(const DevParams&, const Sorted&, uint32_t*, uint32_t*, uint32_t, uint32_t*,
+                                     cudaStream_t);
 
 template void launch_verlet_build<2>(const DevParams&, const State&, const Sorted&, cudaStream_t);
 template void launch_verlet_build<3>(const DevParams&, const State&, const Sorted&, cudaStream_t);

@@ -638,6 +638,7 @@ extern "C" int rrsph_upload(rrsph_solver* s, const double* r, uint32_t stride, c
         s->launches++;
         RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
         s->step_index = 0;
+        s->nlist_valid = false;
         s->keys_ready = true;  // the upload kernel ran the first step's key pass
         return RRSPH_OK;
     }
@@ -680,6 +681,7 @@ int finish_upload(rrsph_solver* s) {
     }
     RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
     s->step_index = 0;
+    s->nlist_valid = false;
     s->keys_ready = false;
     return RRSPH_OK;
 }
@@ -772,6 +774,7 @@ int enqueue_steps(rrsph_solver* s, uint64_t nsteps) {
             if (rc) return rc;
         }
         s->step_index++;
+        s->nlist_valid = s->verlet;  // the step's density pass wrote nlist on the current grid
     }
     return RRSPH_OK;
 }
@@ -891,6 +894,7 @@ namespace {
 template <int DIM>
 void enqueue_component_grid(rrsph_solver* s, bool with_p) {
     s->keys_ready = false;  // this grid's keys were made without the predictor
+    s->nlist_valid = false;  // and it replaces the grid the last step's list refers to
     if (s->S.vl_rebuild) cudaMemsetAsync(s->S.vl_rebuild, 0xFF, sizeof(uint32_t), s->stream);
     rrsph::GatherSrc fsrc{s->S.vx, s->S.vy, s->S.vz, s->S.rho, with_p ? s->S.p : nullptr, 0};
     enqueue_grid<DIM>(s, 0, s->scal, fsrc);
@@ -961,6 +965,46 @@ extern "C" int rrsph_neighbours(rrsph_solver* s, uint32_t* counts, uint32_t* lis
     return rc;
 }
 
+extern "C" int rrsph_step_neighbours(rrsph_solver* s, uint32_t* counts, uint32_t* list, uint32_t max_per,
+                                     uint64_t* total_pairs) {
+    int rc = check_handle(s, "rrsph_step_neighbours");
+    if (rc) return rc;
+    if (!counts || !list || max_per == 0)
+        return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_step_neighbours: bad arguments");
+    if (!s->verlet)
+        return set_error(RRSPH_ERR_UNSUPPORTED, "rrsph_step_neighbours: needs the FP32-mixed step with neighbour reuse");
+    if (!s->nlist_valid)
+        return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_step_neighbours: no step has run since the last upload, "
+                                                     "grid call or reuse setting");
+    cudaStream_t st = s->stream;
+    const size_t n = s->P.n;
+    RRSPH_CUDA_TRY(cudaMemsetAsync(s->flags, 0, sizeof(uint32_t), st));
+    uint32_t *d_counts = nullptr, *d_list = nullptr;
+    RRSPH_CUDA_TRY(cudaMallocAsync(&d_counts, n * sizeof(uint32_t), st));
+    RRSPH_CUDA_TRY(cudaMallocAsync(&d_list, n * (size_t)max_per * sizeof(uint32_t), st));
+    s->G.key = s->G.keys_a;  // the grid of the last rebuild, which the list refers to
+    s->G.id = s->G.ids_a;
+    if (s->dim == 3) rrsph::launch_nlist_export<3>(s->P, s->G, d_counts, d_list, max_per, s->flags, st);
+    else rrsph::launch_nlist_export<2>(s->P, s->G, d_counts, d_list, max_per, s->flags, st);
+    s->launches++;
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(counts, d_counts, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(list, d_list, n * (size_t)max_per * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    RRSPH_CUDA_TRY(cudaFreeAsync(d_counts, st));
+    RRSPH_CUDA_TRY(cudaFreeAsync(d_list, st));
+    RRSPH_CUDA_TRY(cudaMemcpyAsync(s->h_flags, s->flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
+    RRSPH_CUDA_TRY(cudaGetLastError());
+    if (*s->h_flags & RRSPH_FLAG_NEIGHBOUR_OVERFLOW)
+        return set_error(RRSPH_ERR_NEIGHBOUR_OVERFLOW, "rrsph_step_neighbours: a particle has more than max_per "
+                                                       "neighbours, or more than a list holds");
+    if (total_pairs) {
+        uint64_t t = 0;
+        for (size_t j = 0; j < n; j++) t += counts[j];
+        *total_pairs = t;
+    }
+    return RRSPH_OK;
+}
+
 extern "C" int rrsph_density(rrsph_solver* s, double* out_rho_or_drho, double* out_p) {
     int rc = check_handle(s, "rrsph_density");
     if (rc) return rc;
@@ -1001,6 +1045,27 @@ extern "C" int rrsph_forces(rrsph_solver* s, uint32_t terms, double* a, uint32_t
     if (av) RRSPH_CUDA_TRY(cudaMemcpyAsync(av, dv, n * stride * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (mu) RRSPH_CUDA_TRY(cudaMemcpyAsync(mu, s->S.mu, n * sizeof(double), cudaMemcpyDeviceToHost, st));
     return finish_component(s, "rrsph_forces");
+}
+
+extern "C" int rrsph_download_rates(rrsph_solver* s, double* a, uint32_t stride, double* drho) {
+    int rc = check_handle(s, "rrsph_download_rates");
+    if (rc) return rc;
+    if (a && stride < (uint32_t)s->dim) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_download_rates: stride < dim");
+    cudaStream_t st = s->stream;
+    const size_t n = s->P.n;
+    if (a) {
+        if ((rc = ensure_staging(s, n * stride)) != 0) return rc;
+        rrsph::State tmp = s->S;
+        tmp.rx = s->S.ax; tmp.ry = s->S.ay; tmp.rz = s->S.az;
+        if (s->dim == 3) rrsph::launch_pack<3>(s->P, tmp, s->staging, nullptr, stride, st);
+        else rrsph::launch_pack<2>(s->P, tmp, s->staging, nullptr, stride, st);
+        s->launches++;
+        RRSPH_CUDA_TRY(cudaMemcpyAsync(a, s->staging, n * stride * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
+    if (drho) RRSPH_CUDA_TRY(cudaMemcpyAsync(drho, s->S.drho, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
+    RRSPH_CUDA_TRY(cudaGetLastError());
+    return RRSPH_OK;
 }
 
 // ------------------------------------------------------------- timing ------
@@ -1063,6 +1128,7 @@ extern "C" int rrsph_set_neighbour_reuse(rrsph_solver* s, int enable, double ski
         return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_set_neighbour_reuse: skin must be in (0, 1] hsml");
     drop_graphs(s);
     s->verlet = enable != 0;
+    s->nlist_valid = false;
     if (enable) {
         s->verlet_skin = skin_over_h;
         set_verlet_params(s);
@@ -1119,6 +1185,7 @@ int restore_state(rrsph_solver* s, const Backup& b) {
     RRSPH_CUDA_TRY(cudaStreamSynchronize(s->stream));
     s->step_index = b.step_index;
     s->keys_ready = false;
+    s->nlist_valid = false;
     return RRSPH_OK;
 }
 

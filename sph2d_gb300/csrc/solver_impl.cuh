@@ -65,6 +65,7 @@ struct rrsph_solver {
     float4* v4buf[2] = {nullptr, nullptr};
     float4* vd4buf[2] = {nullptr, nullptr};  // continuity density
     unsigned long long vl_extra_launches = 0;  // launches a rebuild adds to a reuse step
+    bool nlist_valid = false;  // nlist / ncount hold the last step's neighbours on the current grid
 };
 
 namespace rrsph_impl {

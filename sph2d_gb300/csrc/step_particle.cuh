@@ -58,8 +58,7 @@ __device__ __forceinline__ void reuse_copies(const DevParams& P, const State& S,
     }
     if (G.VD4n) {
         v.w = d2f(S.rho_pred[i]);
-        G.VD4n[k] = make_float4(d2f(S.vx[i]), d2f(S.vy[i]), DIM == 3 ? d2f(S.vz[i]) : 0.0f,
-                                d2f(S.rho[i] - P.rho0));
+        G.VD4n[k] = vd4_of<DIM>(S.vx[i], S.vy[i], DIM == 3 ? S.vz[i] : 0.0, S.rho[i] - P.rho0);
     }
     G.V4n[k] = v;
 }

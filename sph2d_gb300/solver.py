@@ -143,6 +143,13 @@ class Solver:
         check(lib().rrsph_download(self._h, _dp(r), self.dim, _dp(v), _dp(rho), _dp(pres), _i32p(itype)))
         return {"r": r, "v": v, "rho": rho, "p": pres, "itype": itype}
 
+    def download_rates(self) -> dict:
+        """Accelerations and drho of the last completed step (rrsph_download_rates)."""
+        a = np.zeros((self.n, self.dim))
+        drho = np.zeros(self.n)
+        check(lib().rrsph_download_rates(self._h, _dp(a), self.dim, _dp(drho)))
+        return {"a": a, "drho": drho}
+
     def step(self, nsteps: int, time: float = 0.0) -> float:
         t = C.c_double(time)
         check(lib().rrsph_step(self._h, nsteps, C.byref(t)))
@@ -205,6 +212,17 @@ class Solver:
         lst = np.zeros(self.n * max_per, dtype=np.uint32)
         tot = C.c_uint64()
         check(lib().rrsph_neighbours(self._h, _u32p(counts), _u32p(lst), max_per, C.byref(tot)))
+        return counts, lst.reshape(self.n, max_per), int(tot.value)
+
+    def step_neighbours(self, max_per: int | None = None):
+        """The pairs the last FP32-mixed reuse step's density pass used
+        (rrsph_step_neighbours): counts, list[n, max_per] in the list's own
+        order, total."""
+        max_per = int(max_per or self.params.max_neighbours)
+        counts = np.zeros(self.n, dtype=np.uint32)
+        lst = np.zeros(self.n * max_per, dtype=np.uint32)
+        tot = C.c_uint64()
+        check(lib().rrsph_step_neighbours(self._h, _u32p(counts), _u32p(lst), max_per, C.byref(tot)))
         return counts, lst.reshape(self.n, max_per), int(tot.value)
 
     def density(self):
