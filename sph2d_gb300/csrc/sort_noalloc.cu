@@ -14,6 +14,7 @@
 // exits. Nothing in it needs clearing between calls: every pass rewrites the
 // counts it reads. All calls on a device share it, so calls that can overlap on
 // the GPU race; the caller orders them (one stream, or events).
+#include <cstdint>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -38,7 +39,9 @@ std::mutex g_mutex;
 uint32_t* g_scratch_addr[kMaxDevices] = {};
 
 // Device address of g_sort_scratch on the current device, looked up once per
-// device (with that device current).
+// device (with that device current) and kept for the life of the process: a
+// cudaDeviceReset of that device invalidates it, so the entry point must not
+// be used on a device after a reset.
 int scratch_address(uint32_t** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -60,6 +63,13 @@ int scratch_address(uint32_t** out) {
     return RRSPH_OK;
 }
 
+// Whether [a, a + n) and [b, b + n) (32-bit words) share a word.
+bool overlaps(const void* a, const void* b, uint32_t n) {
+    const uintptr_t x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
+    const uintptr_t len = (uintptr_t)n * sizeof(uint32_t);
+    return x < y + len && y < x + len;
+}
+
 }  // namespace
 
 extern "C" int rrsph_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* ids_in, uint32_t* keys_out,
@@ -74,15 +84,24 @@ extern "C" int rrsph_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t*
     if (n == 0) return RRSPH_OK;
     if (!keys_in || !ids_in || !keys_out || !ids_out)
         return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_sort_pairs_noalloc: null pointer");
-    if (keys_out == keys_in || ids_out == ids_in || keys_out == ids_out)
-        return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_sort_pairs_noalloc: outputs must not overlap the inputs");
+    // the passes write an output while other blocks still read the inputs, and
+    // the two outputs alternate with the working array
+    if (overlaps(keys_out, keys_in, n) || overlaps(keys_out, ids_in, n) || overlaps(ids_out, keys_in, n) ||
+        overlaps(ids_out, ids_in, n) || overlaps(keys_out, ids_out, n))
+        return set_error(RRSPH_ERR_INVALID_ARGUMENT,
+                         "rrsph_sort_pairs_noalloc: the output buffers must not overlap the inputs or each other");
     uint32_t* base = nullptr;
     int rc = scratch_address(&base);
     if (rc) return rc;
-    cudaGetLastError();  // clear an unrelated earlier launch error
+    // an error left by the caller's earlier work is reported, not cleared: its
+    // owner's own check still sees it
+    cudaError_t e = cudaPeekAtLastError();
+    if (e != cudaSuccess)
+        return set_error(RRSPH_ERR_CUDA, std::string("rrsph_sort_pairs_noalloc: an earlier CUDA error is pending: ") +
+                                             cudaGetErrorString(e));
     rrsph::radix_sort_pairs_into(keys_in, ids_in, keys_out, ids_out, base, base + kMaxPairs, base + 2 * (size_t)kMaxPairs,
                                  n, (int)key_bits, static_cast<cudaStream_t>(stream), nullptr);
-    const cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();  // this call's own launches
     if (e != cudaSuccess)
         return set_error(RRSPH_ERR_CUDA, std::string("rrsph_sort_pairs_noalloc: launch: ") + cudaGetErrorString(e));
     return RRSPH_OK;
