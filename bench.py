@@ -41,18 +41,24 @@ UNIT = "pair-interactions/s"
 L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
 
 # Algorithmic bytes of the dominant kernel, k_forces_verlet of the FP32-mixed
-# 2D step with neighbour reuse: the force gather with the whole step fused in.
-# Per particle, the gather reads id 4, position+type float4 16,
-# velocity+pressure+density float4 16, (p, p/rho^2) float2 8, candidate and
-# neighbour counts 4 + 4 and writes a.x, a.y doubles 16; the whole step reads
-# r, v doubles 32, itype 4, key_of 4, build cell 4, build offset 8, build slot 4
-# and writes r, v 32, v_predict float2 8, cell offset float2 8, cell 4, key_of
-# 4, sort key + id 8, the next step's position and velocity float4s 32 and one
-# cell-table word 4. Per neighbour pair it reads one 4-byte word of this step's
-# neighbour list. The neighbours' own data are re-reads of particles other
-# threads load (L1/L2), not algorithmic bytes.
-FORCES_REUSE_BYTES_PER_PARTICLE = (52 + 16) + (32 + 4 + 4 + 4 + 8 + 4) + (32 + 8 + 8 + 4 + 4 + 8 + 32 + 4)
-FORCES_REUSE_BYTES_PER_PAIR = 4
+# 2D step with neighbour reuse (the force gather with the whole step and the
+# next step's key pass fused in), by the per-particle figures of the scope
+# table's roofline: force gather 64 B (read position, velocity, density,
+# pressure, type; write a, drho), integrate + piston 96 B (read and write r, v
+# in FP64, rho, a) and key pass 24 B (read r, write key and id): 184 B per
+# particle. Neighbour data other threads also load are not algorithmic bytes.
+FORCES_ALGORITHMIC_BYTES_PER_PARTICLE = 64 + 96 + 24
+# What the kernel as built reads and writes once per particle and per pair
+# (its own design's bytes, stated beside the algorithmic ones): per particle the
+# gather reads id 4, position+type float4 16, velocity+pressure+density float4
+# 16, (p, p/rho^2) float2 8, candidate and neighbour counts 4 + 4 and writes a.x,
+# a.y doubles 16; the whole step reads r, v doubles 32, itype 4, key_of 4, build
+# cell 4, build offset 8, build slot 4 and writes r, v 32, v_predict float2 8,
+# cell offset float2 8, cell 4, key_of 4, sort key + id 8, the next step's
+# position and velocity float4s 32 and one cell-table word 4; per pair one
+# 4-byte word of this step's neighbour list.
+FORCES_DESIGN_BYTES_PER_PARTICLE = (52 + 16) + (32 + 4 + 4 + 4 + 8 + 4) + (32 + 8 + 8 + 4 + 4 + 8 + 32 + 4)
+FORCES_DESIGN_BYTES_PER_PAIR = 4
 # Pair arithmetic of the FP32 pipe per directed pair: 16 flops for the density
 # (distance, kernel, sum) and 52 for the forces (form-2 pressure term,
 # artificial viscosity, Lennard-Jones amortised); the nominal FP32 (non-tensor)
@@ -62,20 +68,44 @@ FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 FORCES_FP64_BYTES_PER_PARTICLE_2D = 4 + 4 + 16 + 4 + 16 + 8 + 8 + 16
 
 
-def workload_config(case, p, pairs):
+def workload_config(case, pairs_first: int, warmup: int, steps: int) -> dict:
+    """The workload both arms run (the GPU arm and the reference's CPU code):
+    the same seeded particles, parameters and step window."""
     return {
         "workload": "2D piston wave flume: 20 m x 0.5 m water (4000 x 100 at dx=0.005 m), 1.2 m tank, "
                     "LJ walls + piston at dx/2, summation density, piston 0.05*sin(2*pi*t/1.5 s)",
         "n_particles": int(case.ntotal),
         "n_fluid": int(case.notes["nfluid"]),
-        "pairs_per_step": int(pairs),
         "h": case.notes["h"],
         "dt": case.notes["dt"],
-        "precision": "mixed (f32 pairs, f64 state/integration)",
-        "neighbour_search": "candidate lists within cutoff + 0.3 h, rebuilt when a particle has moved 0.15 h",
-        "l2": "flushed (256 MiB device write) before every timed step",
+        "pairs_first_step": int(pairs_first),
+        "window": f"steps {warmup + 1}-{warmup + steps} of the run from the seeded start "
+                  f"(its start-up transient included)",
         "parallelism": "replicas",
     }
+
+
+GPU_METHOD = {
+    "precision": "mixed (f32 pairs, f64 state/integration)",
+    "neighbour_search": "candidate lists within cutoff + 0.3 h, rebuilt when a particle has moved 0.15 h",
+    "l2": "flushed (256 MiB device write) before every timed step",
+}
+
+
+def load_cases():
+    """sph2d_gb300/cases.py (the seeded workload generators, numpy only) loaded
+    as a plain module, without importing the sph2d_gb300 package or loading its
+    library: the reference arm generates the same particles with it."""
+    import importlib.util
+
+    name = "rrsph_workload_cases"
+    if name in sys.modules:
+        return sys.modules[name]
+    spec = importlib.util.spec_from_file_location(name, ROOT / "sph2d_gb300" / "cases.py")
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
 
 
 # --------------------------------------------------------------- clocks ----
@@ -212,7 +242,10 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     sm = Solver(p, "mixed")
     sm.upload(case.r, case.v, case.rho, case.itype)
     sm.set_time(0.0)
-    sm.step_async(args.warmup)
+    sm.step_async(1)
+    sm.sync()
+    pairs_first = sm.pair_count()[0]  # the pairs of the seeded start, which both arms state
+    sm.step_async(args.warmup - 1)
     sm.sync()
     clocks = ClockSampler(local_rank)
     diag0 = sm.diagnostics()
@@ -248,28 +281,37 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     _, q1 = s64.pair_count()
     phases_fp64 = _phase_pass(s64, flush, min(steps64, 10))
 
-    # ---- error of the mixed step against the FP64 GPU step (same start, same steps)
-    err_steps = 50
-    errors = {}
-    for name, s in (("mixed", sm), ("fp64", s64)):
-        s.upload(case.r, case.v, case.rho, case.itype)
-        s.step(err_steps, 0.0)
-    a, b = sm.download(), s64.download()
-    for k in ("r", "v", "rho", "p"):
-        errors[k] = _rel(a[k], b[k])
-    sm.upload(case.r, case.v, case.rho, case.itype)
-    s64.upload(case.r, case.v, case.rho, case.itype)
-    sm.step(1, 0.0)
-    s64.step(1, 0.0)
-    a, b = sm.download(), s64.download()
-    errors_1 = {k: _rel(a[k], b[k]) for k in ("r", "v", "rho", "p")}
+    # ---- error of the mixed step against the FP64 GPU step (same start, same
+    # steps), every field the step writes: state r, v, rho, p and the rates a
+    # (accelerations) and drho (zero here: summation density; the continuity
+    # rate is stated on the dam break below)
+    def _errors(nsteps):
+        out = []
+        for s in (sm, s64):
+            s.upload(case.r, case.v, case.rho, case.itype)
+            s.step(nsteps, 0.0)
+            out.append({**s.download(), **s.download_rates()})
+        a, b = out
+        e = {k: _rel(a[k], b[k]) for k in ("r", "v", "rho", "p", "a")}
+        e["drho"] = None
+        return e
 
-    # ---- end to end through the C ABI with pinned host buffers
+    err_steps = 50
+    errors_1 = _errors(1)
+    errors = _errors(err_steps)
+    errors_cont = continuity_rate_error()
+
+    # ---- end to end through the C ABI with pinned host buffers: each step is
+    # one call of the drop-in boundary on host arrays (rrsph_upload of the
+    # state, rrsph_step(1), rrsph_download of the new state), and the next step
+    # uploads the state the last one downloaded, so the run advances and its
+    # list rebuilds fall inside the timed region (as the reference's
+    # time_integration would run if called for one step at a time: fresh work
+    # arrays at every call)
     pin = lambda x: torch.from_numpy(np.ascontiguousarray(x)).pin_memory().numpy()  # noqa: E731
-    hr, hv, hrho, hit = pin(case.r), pin(case.v), pin(case.rho), pin(case.itype)
     n = case.ntotal
-    out = {k: pin(np.zeros_like(x)) for k, x in (("r", case.r), ("v", case.v), ("rho", case.rho), ("p", case.rho),
-                                                  ("itype", case.itype))}
+    host = {"r": pin(case.r), "v": pin(case.v), "rho": pin(case.rho), "p": pin(np.zeros(n)),
+            "itype": pin(case.itype)}
     import ctypes as C
 
     from sph2d_gb300 import capi
@@ -277,26 +319,32 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     L = capi.lib()
     dp = lambda x: x.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
     ip = lambda x: x.ctypes.data_as(C.POINTER(C.c_int32))  # noqa: E731
-    def e2e_step():
-        capi.check(L.rrsph_upload(sm.handle, dp(hr), 2, dp(hv), dp(hrho), None, ip(hit)))
-        tt = C.c_double(0.0)
-        capi.check(L.rrsph_step(sm.handle, 1, C.byref(tt)))
-        capi.check(L.rrsph_download(sm.handle, dp(out["r"]), 2, dp(out["v"]), dp(out["rho"]), dp(out["p"]),
-                                    ip(out["itype"])))
+    e2e_time = [0.0]
 
-    # as many steps as the timed device loop, at most 200 (~70 ms): one stall of
-    # the host weighs little in the mean
+    def e2e_step():
+        capi.check(L.rrsph_upload(sm.handle, dp(host["r"]), 2, dp(host["v"]), dp(host["rho"]), dp(host["p"]),
+                                  ip(host["itype"])))
+        tt = C.c_double(e2e_time[0])
+        capi.check(L.rrsph_step(sm.handle, 1, C.byref(tt)))
+        e2e_time[0] = tt.value
+        capi.check(L.rrsph_download(sm.handle, dp(host["r"]), 2, dp(host["v"]), dp(host["rho"]), dp(host["p"]),
+                                    ip(host["itype"])))
+        return sm.pair_count()[0]
+
+    # as many steps as the timed device loop, at most 200: one stall of the
+    # host weighs little in the mean
     e2e_steps = max(5, min(args.steps, 200))
     for _ in range(max(3, args.warmup)):
         e2e_step()
+    rb0 = sm.neighbour_rebuilds()
     torch.cuda.synchronize()
+    e2e_pairs = 0
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        e2e_step()
+        e2e_pairs += e2e_step()
     e2e_s = time.perf_counter() - t0
-    # every e2e step starts from the same uploaded state, so it has the same pairs
-    e2e_pairs = e2e_steps * sm.pair_count()[0]
-    h2d = n * (2 * 8 + 2 * 8 + 8 + 4)
+    e2e_rebuilds = sm.neighbour_rebuilds() - rb0
+    h2d = n * (2 * 8 + 2 * 8 + 8 + 8 + 4)
     d2h = n * (2 * 8 + 2 * 8 + 8 + 8 + 4)
 
     # ---- aggregate over ranks (max time, summed pairs)
@@ -315,8 +363,9 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
 
     fkey = "forces"
     f_ms = phases_mixed[fkey]
-    bytes_launch = FORCES_REUSE_BYTES_PER_PARTICLE * n + FORCES_REUSE_BYTES_PER_PAIR * last_pairs
+    bytes_launch = FORCES_ALGORITHMIC_BYTES_PER_PARTICLE * n
     achieved = bytes_launch / (f_ms * 1e-3) / 1e9
+    design_bytes = FORCES_DESIGN_BYTES_PER_PARTICLE * n + FORCES_DESIGN_BYTES_PER_PAIR * last_pairs
     traffic = _profile_traffic()
     result = {
         "metric": METRIC,
@@ -333,7 +382,9 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         "vs_baseline": None,
         "dtype": "f32-pairs/f64-state",
         "data": "synthetic (seeded flume particles of the workload's shape)",
-        "config": workload_config(case, p, last_pairs),
+        "config": workload_config(case, pairs_first, args.warmup, args.steps),
+        "method": GPU_METHOD,
+        "pairs_last_timed_step": int(last_pairs),
         "fp64_step": {
             "ms_per_step": ms_fp64 / steps64,
             "pair_interactions_per_s": (q1 - q0) / (ms_fp64 / 1e3),
@@ -341,7 +392,11 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
             "mixed_speedup": (ms_fp64 / steps64) / (ms_mixed / args.steps),
             "phases_ms_per_step": phases_fp64,
         },
-        "error_vs_fp64_gpu": {"after_1_step": errors_1, f"after_{err_steps}_steps": errors, "metric": "relative L2"},
+        "error_vs_fp64_gpu": {"after_1_step": errors_1, f"after_{err_steps}_steps": errors,
+                              "continuity_dam_break": errors_cont, "metric": "relative L2",
+                              "note": "a = accelerations of the last step; drho is zero on the flume "
+                                      "(summation density) and stated on the 2D dam break with continuity "
+                                      "density and delta-SPH"},
         "phases_ms_per_step": phases_mixed,
         "roofline": {
             "bound": "hbm",
@@ -353,7 +408,14 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
             "peak_source": peak_src,
             "traffic": traffic,
             "algorithmic_bytes_per_launch": bytes_launch,
+            "algorithmic_bytes_per_particle": FORCES_ALGORITHMIC_BYTES_PER_PARTICLE,
             "avg_launch_ms": f_ms,
+            "design_bytes_per_launch": design_bytes,
+            "design_gbs": design_bytes / (f_ms * 1e-3) / 1e9,
+            "step_frac": 390 * n / (ms_mixed / args.steps * 1e-3) / 1e9 / hbm_peak,
+            "note": "achieved = 184 B x particles (force 64 + integrate/piston 96 + key pass 24) / the launch's "
+                    "CUDA-event time; design_gbs counts the kernel's own list words and next-step copies; "
+                    "step_frac = 390 B x particles per step (the whole step's algorithmic bytes) / ms_per_step",
         },
         "fp32_pipe": {
             "flops_per_pair": FLOPS_PER_PAIR,
@@ -364,7 +426,9 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
             "note": "whole mixed step; the gathers are latency-bound on L1/L2 neighbour loads (ncu in profiles/)",
         },
         "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "steps": e2e_steps, "path": "rrsph_upload + rrsph_step(1) + rrsph_download, pinned host buffers"},
+                "steps": e2e_steps, "rebuilds": e2e_rebuilds,
+                "path": "rrsph_upload + rrsph_step(1) + rrsph_download per step on pinned host buffers, each "
+                        "step uploading the state the last one downloaded"},
         "gpu_launches": launches,
         "checks": {
             "fluid_mass_exact": diag1["mass"] == diag0["mass"],
@@ -612,68 +676,99 @@ def _profile_traffic():
 
 # ---------------------------------------------------------- CPU arms -------
 
-def cpu_baseline(case, p, steps: int = 3) -> dict:
-    """The CPU oracle (a C restatement of RRSPH_OMP's step) on all host cores,
-    for a bounded sample of the same workload."""
+def continuity_rate_error(steps: int = 1) -> dict:
+    """Per-field error of the FP32-mixed step against the FP64 GPU step on the
+    2D dam break with continuity density and delta-SPH (coefficient 0.1), after
+    `steps` steps from the seeded start: r, v, rho, p, a and drho."""
+    from sph2d_gb300 import Solver, cases
+
+    case = cases.dam_break_2d(density_treatment=1)
+    p = case.params()
+    p.density_treatment = 2
+    p.density_delta_sph_coef = 0.1
+    out = []
+    for prec in ("mixed", "fp64"):
+        with Solver(p, prec) as s:
+            s.upload(case.r, case.v, case.rho, case.itype)
+            s.step(steps, 0.0)
+            out.append({**s.download(), **s.download_rates()})
+    a, b = out
+    return {k: _rel(a[k], b[k]) for k in ("r", "v", "rho", "p", "a", "drho")}
+
+
+def reference_timing(case, p, warmup: int, steps: int) -> dict:
+    """The reference's CPU implementation of the step on all host cores, over
+    `warmup` untimed and `steps` timed steps from the seeded start: the
+    reference's own RRSPH_OMP compute core (oracle/_ref/rrsph_ref, built from
+    its sources) where it was built, else the C restatement of it (oracle/).
+    Time = the sum of the timed steps' wall times (no I/O)."""
     from oracle import binding as O
 
-    O.set_threads(os.cpu_count() or 1)
-    O.run(p, case.r, case.v, case.rho, case.itype, nsteps=1)  # warm-up (page-in, OpenMP pool)
-    t0 = time.perf_counter()
-    res = O.run(p, case.r, case.v, case.rho, case.itype, nsteps=steps)
-    dt = time.perf_counter() - t0
-    return {"value": res["pairs"] * steps / dt, "unit": UNIT, "cores": O.threads(), "kind": "port",
-            "sample": f"{steps} full steps of the {case.ntotal}-particle flume (directed pairs of the last step "
-                      f"x steps / wall time), oracle/rrsph_oracle.c with OpenMP",
-            "ms_per_step": dt / steps * 1e3}
+    threads = os.cpu_count() or 1
+    total = warmup + steps
+    if O.ref_available():
+        out = O.ref_run(p, f"run:{total}", case.r, case.v, case.rho, case.itype, threads=threads, timeout=3600)
+        step_ms = out["step_ms"]
+        pairs = out["pairs"].astype(np.int64)
+        cores = int(out["timing"]["threads"])
+        kind = "reference"
+        what = "the reference's RRSPH_OMP compute core built from its sources (oracle/_ref/rrsph_ref)"
+    else:
+        O.set_threads(threads)
+        res = O.run(p, case.r, case.v, case.rho, case.itype, nsteps=warmup) if warmup else None
+        st = res or {"r": case.r, "v": case.v, "rho": case.rho, "itype": case.itype, "p": None, "a": None,
+                     "drho": None, "time": 0.0, "pairs_each": np.zeros(0, dtype=np.uint64)}
+        t0 = time.perf_counter()
+        res2 = O.run(p, st["r"], st["v"], st["rho"], st["itype"], nsteps=steps, time=st["time"], pres=st["p"],
+                     a=st["a"], drho=st["drho"], itimestep=warmup)
+        wall_ms = (time.perf_counter() - t0) * 1e3
+        pairs = np.concatenate([st["pairs_each"], res2["pairs_each"]]).astype(np.int64)
+        step_ms = np.concatenate([np.zeros(warmup), np.full(steps, wall_ms / steps)])
+        cores = O.threads()
+        kind = "port"
+        what = "the C restatement of RRSPH_OMP (oracle/rrsph_oracle.c, OpenMP)"
+    t_ms = float(np.sum(step_ms[warmup:total]))
+    timed_pairs = int(np.sum(pairs[warmup:total]))
+    return {"kind": kind, "cores": cores, "ms_per_step": t_ms / steps, "value": timed_pairs / (t_ms / 1e3),
+            "pairs_first": int(pairs[0]), "pairs_timed": timed_pairs,
+            "sample": f"steps {warmup + 1}-{total} of the {case.ntotal}-particle flume from the seeded start on "
+                      f"{cores} threads: {what}; directed pairs of those steps / the sum of their wall times"}
+
+
+def cpu_baseline(case, p, steps: int) -> dict:
+    """The reference's CPU step beside the GPU arm: a bounded sample of the
+    same workload (its first `steps` steps after one warm-up step)."""
+    r = reference_timing(case, p, 1, steps)
+    return {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": r["kind"], "sample": r["sample"],
+            "ms_per_step": r["ms_per_step"]}
 
 
 def run_reference(args, rank: int, world: int) -> dict | None:
-    """The reference's CPU implementation of the step on the host cores: the
-    reference core (oracle/_ref) where it was built, else the C oracle port."""
+    """The reference arm: the reference's CPU implementation of the step on the
+    host cores, on the same workload and step window as the GPU arm. It loads
+    neither the sph2d_gb300 package nor its library: the particles come from
+    the workload generator loaded as a plain module, the parameters from the
+    oracle's own restatement of the reference's loading (oracle/params.py)."""
     if rank != 0:
         return None
-    from sph2d_gb300 import build
+    from oracle import build as ob
 
-    build.build_oracle()
-    from oracle import binding as O
-    from sph2d_gb300 import cases
+    ob.build_all()
+    from oracle import params as OP
 
+    cases = load_cases()
     case = cases.piston_flume_2d()
-    p = case.params()
-    threads = os.cpu_count() or 1
-    steps = max(1, min(args.steps, args.cpu_steps))
-    warm = 1 if args.warmup > 0 else 0
-    if O.ref_available():
-        kind = "reference"
-        if warm:
-            O.ref_run(p, f"run:{warm}", case.r, case.v, case.rho, case.itype, threads=threads)
-        t0 = time.perf_counter()
-        out = O.ref_run(p, f"run:{steps}", case.r, case.v, case.rho, case.itype, threads=threads)
-        wall = time.perf_counter() - t0
-        ms = out["timing"]["total_ms"] / steps
-        pairs = O.run(p, out["r_out"], out["v_out"], out["rho_out"], out["itype_out"], nsteps=1)["pairs"]
-        cores = int(out["timing"]["threads"])
-        del wall
-    else:
-        kind = "port"
-        O.set_threads(threads)
-        if warm:
-            O.run(p, case.r, case.v, case.rho, case.itype, nsteps=warm)
-        t0 = time.perf_counter()
-        res = O.run(p, case.r, case.v, case.rho, case.itype, nsteps=steps)
-        ms = (time.perf_counter() - t0) / steps * 1e3
-        pairs = res["pairs"]
-        cores = O.threads()
-    value = pairs / (ms / 1e3)
-    sample = (f"{steps} full steps of the {case.ntotal}-particle flume on {cores} threads "
-              f"({'reference RRSPH_OMP core built from its sources' if kind == 'reference' else 'C restatement of RRSPH_OMP (oracle)'})")
+    p = OP.case_params(case)
+    r = reference_timing(case, p, args.warmup, args.steps)
+    value = r["value"]
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded flume particles of the workload's shape)",
-        "config": workload_config(case, p, pairs),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+        "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded flume particles of the workload's shape)",
+        "config": workload_config(case, r["pairs_first"], args.warmup, args.steps),
+        "method": {"precision": "f64 (the reference's rr_float)", "neighbour_search": "grid + stencil every step",
+                   "threads": r["cores"]},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": r["cores"], "kind": r["kind"], "sample": r["sample"]},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -684,7 +779,8 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps", type=int, default=50,
+                    help="timed steps of the in-run CPU baseline (the reference's step on the host cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 256-tank ensemble measurement")
     ap.add_argument("--no-dam3d", action="store_true", help="skip the 3D dam break measurement")

@@ -22,7 +22,7 @@ from pathlib import Path
 
 import numpy as np
 
-from sph2d_gb300.capi import RrsphParams
+from .params import OracleParams
 
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "liboracle.so"
@@ -32,7 +32,16 @@ _lib = None
 _dp = C.POINTER(C.c_double)
 _u32p = C.POINTER(C.c_uint32)
 _i32p = C.POINTER(C.c_int32)
-_pp = C.POINTER(RrsphParams)
+_u64p = C.POINTER(C.c_uint64)
+_pp = C.c_void_p
+
+
+def _P(p) -> C.c_void_p:
+    """Address of a params struct: an OracleParams or the GPU library's own
+    ctypes mirror of the same C struct (the sizes are checked)."""
+    if C.sizeof(p) != C.sizeof(OracleParams):
+        raise TypeError(f"params struct of {C.sizeof(p)} bytes, expected {C.sizeof(OracleParams)}")
+    return C.c_void_p(C.addressof(p))
 
 
 def _d(a):
@@ -76,7 +85,7 @@ def lib() -> C.CDLL:
                                   _dp, _dp, _dp]),
             "orc_make_waves": (None, [_pp, _dp, _dp, C.c_uint32, _i32p, C.c_double]),
             "orc_run": (C.c_int, [_pp, _dp, _dp, C.c_uint32, _dp, _dp, _i32p, _dp, _dp, C.c_uint64, C.c_uint64, _dp,
-                                  C.POINTER(C.c_uint64)]),
+                                  _u64p]),
             "orc_gauge": (C.c_double, [_pp, _dp, C.c_uint32, _i32p, C.c_double, C.c_double, C.c_int32]),
             "orc_piston_tangent_run": (C.c_int, [_pp, _dp, _dp, C.c_uint32, _dp, _dp, _i32p, _dp, C.c_uint64, _dp,
                                                  C.c_uint32, C.c_double, _dp, C.c_double, C.c_double, C.c_int32,
@@ -110,18 +119,18 @@ def _chk(rc):
         raise OracleError(f"oracle status {rc}")
 
 
-def grid(p: RrsphParams, r: np.ndarray):
+def grid(p, r: np.ndarray):
     r = np.ascontiguousarray(r, dtype=np.float64)
     n = int(p.ntotal)
     keys = np.zeros(n, dtype=np.uint32)
     g = np.zeros(n, dtype=np.uint32)
     cs = np.zeros(int(p.max_cells) + 1, dtype=np.uint32)
-    _chk(lib().orc_cell_keys(C.byref(p), _d(r), r.shape[1], _u(keys)))
-    _chk(lib().orc_make_grid(C.byref(p), _u(keys), _u(g), _u(cs)))
+    _chk(lib().orc_cell_keys(_P(p), _d(r), r.shape[1], _u(keys)))
+    _chk(lib().orc_make_grid(_P(p), _u(keys), _u(g), _u(cs)))
     return keys, g, cs
 
 
-def neighbours(p: RrsphParams, r, itype, max_per: int | None = None):
+def neighbours(p, r, itype, max_per: int | None = None):
     """(counts, list[n, max_per], grid, cells_start) of find_neighbours."""
     r = np.ascontiguousarray(r, dtype=np.float64)
     itype = np.ascontiguousarray(itype, dtype=np.int32)
@@ -130,12 +139,12 @@ def neighbours(p: RrsphParams, r, itype, max_per: int | None = None):
     max_per = int(max_per or p.max_neighbours)
     counts = np.zeros(n, dtype=np.uint32)
     lst = np.zeros((n, max_per), dtype=np.uint32)
-    _chk(lib().orc_find_neighbours(C.byref(p), _d(r), r.shape[1], _i(itype), _u(g), _u(cs), _u(counts), _u(lst),
+    _chk(lib().orc_find_neighbours(_P(p), _d(r), r.shape[1], _i(itype), _u(g), _u(cs), _u(counts), _u(lst),
                                    max_per))
     return counts, lst, keys, g, cs
 
 
-def density(p: RrsphParams, r, v, rho, itype):
+def density(p, r, v, rho, itype):
     """density_sum (rho, p) or density_con (drho, p) by p.density_treatment."""
     r = np.ascontiguousarray(r, dtype=np.float64)
     v = np.ascontiguousarray(v, dtype=np.float64)
@@ -146,14 +155,14 @@ def density(p: RrsphParams, r, v, rho, itype):
     pres = np.zeros(n)
     mp = lst.shape[1]
     if p.density_treatment == 0:
-        lib().orc_density_sum(C.byref(p), _d(r), r.shape[1], _u(counts), _u(lst), mp, _d(out), _d(pres))
+        lib().orc_density_sum(_P(p), _d(r), r.shape[1], _u(counts), _u(lst), mp, _d(out), _d(pres))
     else:
-        lib().orc_density_con(C.byref(p), _d(r), _d(v), r.shape[1], _d(rho), _u(counts), _u(lst), mp, _d(out),
+        lib().orc_density_con(_P(p), _d(r), _d(v), r.shape[1], _d(rho), _u(counts), _u(lst), mp, _d(out),
                               _d(pres))
     return out, pres
 
 
-def forces(p: RrsphParams, terms: int, r, v, rho, pres, itype):
+def forces(p, terms: int, r, v, rho, pres, itype):
     r = np.ascontiguousarray(r, dtype=np.float64)
     v = np.ascontiguousarray(v, dtype=np.float64)
     rho = np.ascontiguousarray(rho, dtype=np.float64)
@@ -164,18 +173,19 @@ def forces(p: RrsphParams, terms: int, r, v, rho, pres, itype):
     a = np.zeros((n, dim))
     av = np.zeros((n, dim))
     mu = np.zeros(n)
-    lib().orc_forces(C.byref(p), terms, _i(itype), _d(r), _d(v), dim, _d(rho), _d(pres), _u(counts), _u(lst),
+    lib().orc_forces(_P(p), terms, _i(itype), _d(r), _d(v), dim, _d(rho), _d(pres), _u(counts), _u(lst),
                      lst.shape[1], _d(a), _d(av), _d(mu))
     return a, av, mu
 
 
-def eos_p(p: RrsphParams, rho) -> np.ndarray:
-    return np.array([lib().orc_eos_p(C.byref(p), float(x)) for x in np.atleast_1d(rho)])
+def eos_p(p, rho) -> np.ndarray:
+    return np.array([lib().orc_eos_p(_P(p), float(x)) for x in np.atleast_1d(rho)])
 
 
-def run(p: RrsphParams, r, v, rho, itype, nsteps: int, time: float = 0.0, pres=None, a=None, drho=None,
+def run(p, r, v, rho, itype, nsteps: int, time: float = 0.0, pres=None, a=None, drho=None,
         itimestep: int = 0):
-    """nsteps of the time loop; returns the state dict (r, v, rho, p, itype, a, drho, time, pairs)."""
+    """nsteps of the time loop; returns the state dict (r, v, rho, p, itype, a, drho, time, pairs:
+    the directed pairs of the last step, pairs_each: of every step)."""
     q = p.copy()
     r = np.array(r, dtype=np.float64, order="C")
     v = np.array(v, dtype=np.float64, order="C")
@@ -186,14 +196,14 @@ def run(p: RrsphParams, r, v, rho, itype, nsteps: int, time: float = 0.0, pres=N
     a = np.zeros((n, dim)) if a is None else np.array(a, dtype=np.float64, order="C")
     drho = np.zeros(n) if drho is None else np.array(drho, dtype=np.float64)
     t = C.c_double(time)
-    pairs = C.c_uint64()
-    _chk(lib().orc_run(C.byref(q), _d(r), _d(v), dim, _d(rho), _d(pres), _i(itype), _d(a), _d(drho), itimestep,
-                       nsteps, C.byref(t), C.byref(pairs)))
+    pairs = np.zeros(max(int(nsteps), 1), dtype=np.uint64)
+    _chk(lib().orc_run(_P(q), _d(r), _d(v), dim, _d(rho), _d(pres), _i(itype), _d(a), _d(drho), itimestep,
+                       nsteps, C.byref(t), pairs.ctypes.data_as(_u64p)))
     return {"r": r, "v": v, "rho": rho, "p": pres, "itype": itype, "a": a, "drho": drho, "time": t.value,
-            "pairs": int(pairs.value)}
+            "pairs": int(pairs[nsteps - 1]) if nsteps else 0, "pairs_each": pairs[:nsteps]}
 
 
-def piston_tangent_run(p: RrsphParams, r, v, rho, itype, nsteps: int, omega: float, coef, gauge_x: float,
+def piston_tangent_run(p, r, v, rho, itype, nsteps: int, omega: float, coef, gauge_x: float,
                        search_n: float = 3.0, gauge_type: int = 2, sample_from: int = 0, sample_every: int = 1,
                        time: float = 0.0):
     """Forward run with the Fourier piston X(t) = sum_k coef[k-1] sin(k omega t)
@@ -213,17 +223,17 @@ def piston_tangent_run(p: RrsphParams, r, v, rho, itype, nsteps: int, omega: flo
     dg = np.zeros((max(cap, 1), coef.size))
     t = C.c_double(time)
     ns = C.c_uint64()
-    _chk(lib().orc_piston_tangent_run(C.byref(q), _d(r), _d(v), dim, _d(rho), _d(pres), _i(itype), _d(a), nsteps,
+    _chk(lib().orc_piston_tangent_run(_P(q), _d(r), _d(v), dim, _d(rho), _d(pres), _i(itype), _d(a), nsteps,
                                       C.byref(t), coef.size, float(omega), _d(coef), float(gauge_x), float(search_n),
                                       int(gauge_type), sample_from, sample_every, _d(g), _d(dg), cap, C.byref(ns)))
     k = int(ns.value)
     return g[:k], dg[:k], {"r": r, "v": v, "rho": rho, "p": pres, "itype": itype, "a": a, "time": t.value}
 
 
-def gauge(p: RrsphParams, r, itype, x: float, search_n: float = 3.0, type_filter: int = 0) -> float:
+def gauge(p, r, itype, x: float, search_n: float = 3.0, type_filter: int = 0) -> float:
     r = np.ascontiguousarray(r, dtype=np.float64)
     itype = np.ascontiguousarray(itype, dtype=np.int32)
-    return float(lib().orc_gauge(C.byref(p), _d(r), r.shape[1], _i(itype), float(x), float(search_n),
+    return float(lib().orc_gauge(_P(p), _d(r), r.shape[1], _i(itype), float(x), float(search_n),
                                  int(type_filter)))
 
 
@@ -247,9 +257,15 @@ _REF_KEYS = [
 ]
 
 
-def ref_run(p: RrsphParams, mode: str, r, v, rho, itype, pres=None, threads: int = 0, timeout: float = 600):
+def ref_run(p, mode: str, r, v, rho, itype, pres=None, threads: int = 0, timeout: float = 600,
+            gauges=None):
     """Runs the reference's compute core (oracle/_ref/rrsph_ref) in a child
-    process on this state. Returns a dict of the output arrays."""
+    process on this state. Returns a dict of the output arrays.
+
+    For mode "run:N", ``gauges=(every, search_n, type_filter, xs)`` samples the
+    WaterProfile elevation at the positions xs before the first step and after
+    every ``every`` steps (result "gauges": samples x len(xs)); "pairs" holds the
+    directed pairs of each step's find_neighbours."""
     if not ref_available():
         raise OracleError("reference core not built (oracle/_ref/rrsph_ref)")
     n, dim = int(p.ntotal), int(p.dim)
@@ -258,6 +274,11 @@ def ref_run(p: RrsphParams, mode: str, r, v, rho, itype, pres=None, threads: int
         with open(dd / "params.txt", "w") as f:
             for k in _REF_KEYS:
                 f.write(f"{k} {float(getattr(p, k))!r}\n")
+        if gauges is not None:
+            every, search_n, type_filter, xs = gauges
+            with open(dd / "gauges.txt", "w") as f:
+                f.write(f"{int(every)} {float(search_n)!r} {int(type_filter)}\n")
+                f.write(" ".join(repr(float(x)) for x in xs) + "\n")
         np.ascontiguousarray(r, dtype=np.float64).tofile(dd / "r.f64")
         np.ascontiguousarray(v, dtype=np.float64).tofile(dd / "v.f64")
         np.ascontiguousarray(rho, dtype=np.float64).tofile(dd / "rho.f64")
@@ -269,9 +290,11 @@ def ref_run(p: RrsphParams, mode: str, r, v, rho, itype, pres=None, threads: int
         out = {}
         for f in dd.iterdir():
             name, _, ext = f.name.rpartition(".")
-            if f.name in ("params.txt", "r.f64", "v.f64", "rho.f64", "p.f64", "itype.i32"):
+            if f.name in ("params.txt", "gauges.txt", "r.f64", "v.f64", "rho.f64", "p.f64", "itype.i32"):
                 continue
-            if ext == "f64":
+            if ext == "u64":
+                out[name] = np.fromfile(f, dtype=np.uint64)
+            elif ext == "f64":
                 out[name] = np.fromfile(f, dtype=np.float64)
             elif ext == "u32":
                 out[name] = np.fromfile(f, dtype=np.uint32)
@@ -282,4 +305,6 @@ def ref_run(p: RrsphParams, mode: str, r, v, rho, itype, pres=None, threads: int
         for key in ("a", "av", "r_out", "v_out", "a_out"):
             if key in out:
                 out[key] = out[key].reshape(n, dim)
+        if gauges is not None and "gauges" in out:
+            out["gauges"] = out["gauges"].reshape(-1, len(gauges[3]))
         return out

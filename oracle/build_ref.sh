@@ -1,8 +1,15 @@
 #!/bin/sh
-# Builds the reference's own RRSPH_OMP compute core from its sources, in place,
-# together with oracle/ref_driver.cpp, into oracle/_ref/rrsph_ref (TEST
-# INFRASTRUCTURE: used to pin the C oracle and as the "reference" CPU baseline
-# where the reference sources exist). Outputs go to oracle/_ref/ only.
+# Builds the reference's own RRSPH_OMP compute core from its sources, together
+# with oracle/ref_driver.cpp, into oracle/_ref/rrsph_ref (TEST INFRASTRUCTURE:
+# used to pin the C oracle and as the "reference" CPU baseline). Outputs go to
+# oracle/_ref/ only, which is kept out of version control.
+#
+# Where the reference checkout is present ($RRSPH_REFERENCE, default
+# /root/reference), the few files the core needs are first staged, unchanged,
+# under oracle/_ref/src/sources/ (the include directories of RRSPH_PARAMS,
+# RRSPH_COMMON, RRSPH_OMP and RR, the six compiled .cpp files and the version
+# templates); the core is always compiled from that staged copy, so a machine
+# that has the staged copy but not the checkout builds the same binary.
 #
 # Only the compute core builds here: the reference's executable needs fmt and
 # googletest, which it does not vendor. Two things are generated into
@@ -18,11 +25,30 @@ set -eu
 REF="${RRSPH_REFERENCE:-/root/reference}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
-S="$REF/sources"
-if [ ! -d "$S/RRSPH_OMP/src" ]; then
-    echo "build_ref: reference sources not found under $REF; nothing built"
+STAGE="$OUT/src/sources"
+if [ -d "$REF/sources/RRSPH_OMP/src" ]; then
+    R="$REF/sources"
+    rm -rf "$OUT/src"
+    mkdir -p "$STAGE/RRSPH_OMP/src" "$STAGE/RRSPH_COMMON/src" "$STAGE/RRSPH_PARAMS" "$STAGE/RRSPH_COMMON" \
+             "$STAGE/RRSPH_OMP" "$STAGE/RR"
+    cp -R "$R/RRSPH_PARAMS/include" "$STAGE/RRSPH_PARAMS/"
+    cp -R "$R/RRSPH_COMMON/include" "$STAGE/RRSPH_COMMON/"
+    cp -R "$R/RRSPH_OMP/include" "$STAGE/RRSPH_OMP/"
+    cp -R "$R/RR/include" "$STAGE/RR/"
+    for f in GridFind UpdateAcceleration PredictHalfStep WholeStep WaveMaker; do
+        cp "$R/RRSPH_OMP/src/$f.cpp" "$STAGE/RRSPH_OMP/src/"
+    done
+    cp "$R/RRSPH_COMMON/src/EOS.cpp" "$STAGE/RRSPH_COMMON/src/"
+    cp "$R/RRSPH_PARAMS/ParamsVersion.h.in" "$STAGE/RRSPH_PARAMS/"
+    cp "$R/RRSPHVersion.h.in" "$STAGE/"
+    cp "$R/RRSPH_COMMON/RRSPHCOMMONVersion.h.in" "$STAGE/RRSPH_COMMON/"
+    cp "$R/RRSPH_OMP/RRSPHOMPVersion.h.in" "$STAGE/RRSPH_OMP/"
+    chmod -R u+w "$OUT/src"
+elif [ ! -d "$STAGE/RRSPH_OMP/src" ]; then
+    echo "build_ref: reference sources not found under $REF or $STAGE; nothing built"
     exit 0
 fi
+S="$STAGE"
 mkdir -p "$OUT/gen"
 ver() { sed "s/@PROJECT_VERSION_MAJOR@/$2/;s/@PROJECT_VERSION_MINOR@/$3/;s/@PROJECT_VERSION_PATCH@/$4/" "$1"; }
 ver "$S/RRSPH_PARAMS/ParamsVersion.h.in" 3 1 4 > "$OUT/gen/ParamsVersion.h"
@@ -42,5 +68,6 @@ CXX="${CXX:-g++}"
     "$S/RRSPH_OMP/src/GridFind.cpp" "$S/RRSPH_OMP/src/UpdateAcceleration.cpp" \
     "$S/RRSPH_OMP/src/PredictHalfStep.cpp" "$S/RRSPH_OMP/src/WholeStep.cpp" \
     "$S/RRSPH_OMP/src/WaveMaker.cpp" "$S/RRSPH_COMMON/src/EOS.cpp" \
-    "$HERE/ref_driver.cpp" -o "$OUT/rrsph_ref"
+    "$HERE/ref_driver.cpp" -o "$OUT/rrsph_ref.tmp"
+mv "$OUT/rrsph_ref.tmp" "$OUT/rrsph_ref"
 echo "build_ref: built $OUT/rrsph_ref"

@@ -13,7 +13,13 @@
 //   accel       update_acceleration                   (RRSPH_OMP/src/UpdateAcceleration.cpp:33-125)
 //   run:N       N iterations of the loop body of TimeIntegration.cpp:60-100 with the
 //               piston call enabled (dynamic_boundaries, WaveMaker.cpp:34-82),
-//               reporting wall time per phase
+//               reporting wall time per phase and per step (step_ms.f64) and the
+//               directed pairs of every step's find_neighbours (pairs.u64, counted
+//               outside the timed phases); when
+//               case_dir holds gauges.txt ("every search_n type_filter" then the gauge
+//               x positions), the WaterProfile free-surface elevation at those
+//               positions is sampled before the first step and after every `every`
+//               steps into gauges.f64 (samples x gauges)
 //
 // Usage: rrsph_ref <case_dir> <mode> [threads]
 // Inputs in case_dir: params.txt, r.f64, v.f64, rho.f64, p.f64, itype.i32
@@ -31,7 +37,10 @@
 #include "WholeStep.h"
 #include "WaveMaker.h"
 
+#include <algorithm>
 #include <chrono>
+#include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -243,6 +252,38 @@ void mode_terms(State& s, unsigned mask) {
     write_array("mu.f64", &mu(0), n);
 }
 
+// HeightTesting::maxInLayer (tools/WaterProfile/include/HeightTesting.h:25-54): the
+// largest y over the particles (of type `type_filter` when it is non-zero) with
+// |x - x_gauge| < search_n * hsml; 0 when none is near.
+double gauge_max_in_layer(const State& s, double x_gauge, double search_n, int type_filter) {
+    const double radius = search_n * params.hsml;
+    const auto& r = s.r.get_flt2();
+    double best = 0;
+    for (size_t i = 0; i < params.ntotal; i++) {
+        if (type_filter && s.itype(i) != type_filter) continue;
+        if (std::fabs(r(i).x - x_gauge) < radius) best = std::max(best, r(i).y);
+    }
+    return best;
+}
+
+struct GaugeSpec {
+    unsigned long every = 0;
+    double search_n = 3;
+    int type_filter = 0;
+    std::vector<double> xs;
+};
+
+GaugeSpec load_gauges() {
+    GaugeSpec g;
+    std::ifstream f(g_dir + "/gauges.txt");
+    if (!f) return g;
+    f >> g.every >> g.search_n >> g.type_filter;
+    double x;
+    while (f >> x) g.xs.push_back(x);
+    if (params.dim != 2) throw std::runtime_error("gauges: 2D only");
+    return g;
+}
+
 double ms_since(std::chrono::steady_clock::time_point t0) {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
@@ -308,15 +349,35 @@ int main(int argc, char** argv) {
             vheap_darray_floatn v_predict(params.maxn), a(params.maxn), av(params.maxn);
             heap_darray_md<rr_uint> nb(params.max_neighbours, params.maxn);
             rr_float time = params.start_simulation_time;
-            double t_predict = 0, t_grid = 0, t_density = 0, t_accel = 0, t_whole = 0;
+            double t_predict = 0, t_grid = 0, t_density = 0, t_accel = 0, t_whole = 0, t_aside = 0;
+            const GaugeSpec gs = load_gauges();
+            std::vector<double> gauges;
+            auto sample = [&]() {
+                for (double x : gs.xs) gauges.push_back(gauge_max_in_layer(s, x, gs.search_n, gs.type_filter));
+            };
+            std::vector<uint64_t> pairs(nsteps);
+            std::vector<double> step_ms(nsteps);
+            if (gs.every) sample();
             auto t_all = std::chrono::steady_clock::now();
             for (unsigned long step = 0; step < nsteps; step++) {
+                const double phases_before = t_predict + t_grid + t_density + t_accel + t_whole;
                 auto t0 = std::chrono::steady_clock::now();
                 predict_half_step(s.itype, s.rho, drho, s.v, a, rho_predict, v_predict);
                 t_predict += ms_since(t0);
                 t0 = std::chrono::steady_clock::now();
                 grid_find(s.r, s.itype, nb);
                 t_grid += ms_since(t0);
+                t0 = std::chrono::steady_clock::now();
+                {
+                    uint64_t cnt = 0;
+                    const rr_iter nn = (rr_iter)params.ntotal;
+#pragma omp parallel for reduction(+ : cnt)
+                    for (rr_iter j = 0; j < nn; j++) {
+                        for (rr_iter k = 0; nb(k, j) != params.ntotal; k++) cnt++;
+                    }
+                    pairs[step] = cnt;
+                }
+                t_aside += ms_since(t0);
                 t0 = std::chrono::steady_clock::now();
                 if (cont) density_con(s.r, s.v, nb, s.rho, drho, s.p);
                 else density_sum(s.r, nb, s.rho, s.p);
@@ -332,9 +393,18 @@ int main(int argc, char** argv) {
                 }
                 whole_step(step, drho, a, av, s.itype, s.rho, s.v, s.r);
                 t_whole += ms_since(t0);
+                step_ms[step] = t_predict + t_grid + t_density + t_accel + t_whole - phases_before;
                 time += params.dt;
+                if (gs.every && (step + 1) % gs.every == 0) {
+                    t0 = std::chrono::steady_clock::now();
+                    sample();
+                    t_aside += ms_since(t0);
+                }
             }
-            const double total = ms_since(t_all);
+            const double total = ms_since(t_all) - t_aside;
+            write_array("pairs.u64", pairs.data(), pairs.size());
+            write_array("step_ms.f64", step_ms.data(), step_ms.size());
+            if (gs.every) write_array("gauges.f64", gauges.data(), gauges.size());
             auto fr = flat(s.r), fv = flat(s.v), fa = flat(a);
             write_array("r_out.f64", fr.data(), fr.size());
             write_array("v_out.f64", fv.data(), fv.size());

@@ -620,7 +620,7 @@ static int within_geometry(const rrsph_params* p, const double* q) { /* WholeSte
 int orc_run(rrsph_params* p, double* r, double* v, uint32_t stride, double* rho,
             double* pres, int32_t* itype, double* a, double* drho,
             uint64_t itimestep, uint64_t nsteps, double* time_io,
-            uint64_t* pair_count) {
+            uint64_t* pair_counts) {
     const uint64_t n = p->ntotal;
     const int dim = (int)p->dim;
     const int cont = p->density_treatment != 0;
@@ -657,10 +657,10 @@ int orc_run(rrsph_params* p, double* r, double* v, uint32_t stride, double* rho,
         if (rc) goto done;
         rc = orc_find_neighbours(p, r, stride, itype, grid, cells, counts, list, max_per);
         if (rc) goto done;
-        if (pair_count) {
+        if (pair_counts) {
             uint64_t tot = 0;
             for (uint64_t i = 0; i < n; i++) tot += counts[i];
-            *pair_count = tot;
+            pair_counts[s] = tot;
         }
         /* density */
         if (cont) orc_density_con(p, r, v, stride, rho, counts, list, max_per, drho, pres);

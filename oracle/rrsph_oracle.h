@@ -90,11 +90,12 @@ void orc_make_waves(rrsph_params* p, double* r, double* v, uint32_t stride,
  * drho (ntotal rows each) carry the previous step's values (zero at the start,
  * as the loop's fresh work arrays). itimestep is the loop counter of the first
  * step (0 => dt/2 velocity update, WholeStep.cpp:33). Returns 0 or an RRSPH_ERR_*
- * code. pair_count (may be NULL) receives the directed pairs of the last step. */
+ * code. pair_counts (may be NULL) receives the directed pairs of each step
+ * (nsteps entries). */
 int orc_run(rrsph_params* p, double* r, double* v, uint32_t stride, double* rho,
             double* pres, int32_t* itype, double* a, double* drho,
             uint64_t itimestep, uint64_t nsteps, double* time_io,
-            uint64_t* pair_count);
+            uint64_t* pair_counts);
 
 /* Gauge elevation: HeightTesting::maxInLayer (tools/WaterProfile/include/
  * HeightTesting.h:25-54) — max y of particles with |x - x_gauge| < search_n*h

@@ -1,11 +1,10 @@
 """Builds the native libraries in-tree (no cmake, no pip install).
 
 - ``sph2d_gb300/librrsph_cuda.so``: the CUDA kernels (sm_103a) and the C ABI
-  declared in ``include/rrsph_cuda.h`` (solver, parameters, CSV layers).
-- ``oracle/liboracle.so``: the CPU oracle used by the tests and the benchmark's
-  CPU baseline (plain C + OpenMP, built with ``-ffp-contract=off``).
-- ``oracle/_ref/rrsph_ref``: the reference's own OMP compute core, only where
-  the reference sources are present (``oracle/build_ref.sh``).
+  declared in ``include/rrsph_cuda.h`` (solver, parameters, CSV layers);
+- ``sph2d_gb300/rrsph_run``: the command-line runner linked against it.
+
+The CPU checkers (the oracle) have their own recipe, ``oracle/build.py``.
 
 Translation units compile in parallel; a rebuild is skipped when every output
 is newer than its inputs.
@@ -27,9 +26,6 @@ HOST = PKG / "host"
 BUILD = PKG / "_build"
 LIB = PKG / "librrsph_cuda.so"
 RUNNER = PKG / "rrsph_run"
-ORACLE_DIR = ROOT / "oracle"
-ORACLE_LIB = ORACLE_DIR / "liboracle.so"
-REF_BIN = ORACLE_DIR / "_ref" / "rrsph_ref"
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CU_SOURCES = ["sort.cu", "kernels_common.cu", "kernels_fp64.cu", "kernels_mixed.cu", "kernels_reuse.cu", "solver.cu",
@@ -107,35 +103,10 @@ def build_cuda(verbose: bool = False, extra_nvcc=()) -> Path:
     return LIB
 
 
-def build_oracle(verbose: bool = False) -> Path:
-    """Compiles the C oracle into ``oracle/liboracle.so``."""
-    srcs = [ORACLE_DIR / "rrsph_oracle.c", ORACLE_DIR / "rrsph_tangent.c"]
-    hdrs = [ORACLE_DIR / "rrsph_oracle.h", ROOT / "include" / "rrsph_cuda.h"]
-    if not _newer(ORACLE_LIB, [*srcs, *hdrs]):
-        tmp = ORACLE_LIB.with_suffix(".so.tmp")
-        _run(["gcc", "-std=c11", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-Wall", "-o", tmp,
-              *srcs, "-lm"], verbose)
-        os.replace(tmp, ORACLE_LIB)
-    return ORACLE_LIB
-
-
-def build_reference(verbose: bool = False) -> Path | None:
-    """Builds the reference's compute core when its sources are present."""
-    ref = Path(os.environ.get("RRSPH_REFERENCE", "/root/reference"))
-    if not (ref / "sources" / "RRSPH_OMP" / "src").is_dir():
-        return None
-    if not REF_BIN.exists() or REF_BIN.stat().st_mtime < (ORACLE_DIR / "ref_driver.cpp").stat().st_mtime:
-        _run(["sh", str(ORACLE_DIR / "build_ref.sh")], verbose)
-    return REF_BIN if REF_BIN.exists() else None
-
-
 def build_all(verbose: bool = False) -> None:
-    with cf.ThreadPoolExecutor(max_workers=3) as ex:
-        futs = [ex.submit(build_cuda, verbose), ex.submit(build_oracle, verbose), ex.submit(build_reference, verbose)]
-        for f in futs:
-            f.result()
+    build_cuda(verbose)
 
 
 if __name__ == "__main__":
     build_all(verbose="-v" in sys.argv)
-    print("built", LIB, ORACLE_LIB, REF_BIN if REF_BIN.exists() else "(no reference core)")
+    print("built", LIB, RUNNER)

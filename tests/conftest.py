@@ -1,4 +1,3 @@
-import os
 import sys
 from pathlib import Path
 
@@ -8,7 +7,9 @@ ROOT = Path(__file__).resolve().parent.parent
 if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
 
-REFERENCE = Path(os.environ.get("RRSPH_REFERENCE", "/root/reference"))
+from oracle.build import reference_root  # noqa: E402
+
+REFERENCE = reference_root()
 GOLDEN_CASE = REFERENCE / "sources" / "RRSPH_COMMON" / "tests" / "caseDamBreak"
 
 
@@ -19,11 +20,12 @@ def pytest_configure(config):
 @pytest.fixture(scope="session", autouse=True)
 def _built():
     """Builds the in-tree libraries once per session (incremental)."""
+    from oracle import build as ob
     from sph2d_gb300 import build
 
     build.build_cuda()
-    build.build_oracle()
-    build.build_reference()
+    ob.build_oracle()
+    ob.build_reference()
     yield
 
 

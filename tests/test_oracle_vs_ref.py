@@ -106,3 +106,32 @@ def test_time_loop_matches(name, case):
         assert e <= 1e-12, (k, e)
     assert np.array_equal(mine["itype"], ref["itype_out"])
     assert mine["time"] == pytest.approx(ref["timing"]["time"], rel=1e-12)
+
+
+@pytest.mark.parametrize("nwm, extra", [(3, {}), (4, {"nwm_time_start": 0.0005}), (5, {"nwm_wave_magnitude": 0.05})],
+                         ids=["piston_2nd_order", "wall_disappear", "solitary_rayleigh"])
+def test_wave_makers_match(nwm, extra):
+    """25 steps of the loop with the second-order piston (the OMP sum of
+    WaveMaker.cpp:70), the disappearing wall (WaveMaker.cpp:136-157, which
+    turns itself off after its call) and the solitary-wave piston
+    (WaveMaker.cpp:84-134), against the reference's own make_waves."""
+    from oracle import binding as O
+    from sph2d_gb300 import cases
+
+    case = cases.piston_flume_2d(nx=150, ny=20)
+    p = case.params()
+    p.nwm = nwm
+    for k, v in extra.items():
+        setattr(p, k, v)
+    n = 25
+    mine = O.run(p, case.r, case.v, case.rho, case.itype, nsteps=n)
+    ref = O.ref_run(p, f"run:{n}", case.r, case.v, case.rho, case.itype)
+    for k, rk in (("r", "r_out"), ("v", "v_out"), ("rho", "rho_out"), ("p", "p_out"), ("a", "a_out")):
+        e = rel_l2(mine[k], ref[rk])
+        assert e <= 1e-12, (k, e)
+    assert np.array_equal(mine["itype"], ref["itype_out"])
+    if nwm == 4:
+        assert np.all(mine["itype"][p.nwm_particles_start:p.nwm_particles_end] == 0)
+    else:  # the piston column moved
+        assert not np.array_equal(mine["r"][p.nwm_particles_start:p.nwm_particles_end],
+                                  case.r[p.nwm_particles_start:p.nwm_particles_end])
