@@ -3,7 +3,7 @@ adjoint (rrsph_adjoint_forward/reverse) against central finite differences of
 the FP64 GPU forward run and, where the oracle can afford the run, against the
 oracle's FP64 forward-mode derivatives.
 
-  python -m sph2d_gb300.validate_adjoint [--nx 2000 --ny 100 --steps 5000]
+  python tests/adjoint_check.py [--nx 2000 --ny 100 --steps 5000]
          [--checkpoint-every 100] [--eps 1e-6] [--oracle]
 
 Loss: mean over the samples of (gauge - target)^2, the target series being the

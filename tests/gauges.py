@@ -6,7 +6,7 @@ The gauge is the reference's WaterProfile measure
 particles with |x - x_gauge| < search_n * h (search_n = 3), sampled every
 `--every` steps.
 
-  python -m sph2d_gb300.validate --case flume --steps 20000 --every 200
+  python tests/gauges.py --case flume --steps 20000 --every 200
          [--gauges 2,5,10] [--oracle-steps N] [--out series.csv]
 
 Prints one JSON line with the maximum and mean relative gauge differences:

@@ -1,6 +1,6 @@
 """Runs a few steps of a workload, for profilers (ncu) to capture.
 
-  python -m sph2d_gb300.profile_step [--precision mixed|fp64] [--steps N]
+  python tests/profile_step.py [--precision mixed|fp64] [--steps N]
                                      [--case flume|dam|dam3d] [--nx 4000 --ny 100]
                                      [--dx3d 0.0026] [--no-graph]
 
