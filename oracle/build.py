@@ -72,7 +72,8 @@ def build_reference(verbose: bool = False) -> Path | None:
     the staged copy) are present; returns the binary or None."""
     if not reference_sources_available():
         return None
-    inputs = [HERE / "ref_driver.cpp", HERE / "build_ref.sh"]
+    inputs = [HERE / "ref_driver.cpp", HERE / "build_ref.sh", HERE / "ref_params_driver.cpp",
+              *sorted((ROOT / "sph2d_gb300" / "integration").glob("*"))]
     if not _newer(REF_BIN, inputs):
         env = dict(os.environ)
         env.setdefault("RRSPH_REFERENCE", str(reference_root()))

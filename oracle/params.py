@@ -113,9 +113,11 @@ def defaults() -> OracleParams:
 
 
 def _version_before_3_1_4(js: dict) -> bool:
-    v = (js.get("params_target_version_major", 0), js.get("params_target_version_minor", 0),
-         js.get("params_target_version_patch", 0))
-    return tuple(int(x) for x in v) < (3, 1, 4)
+    """target < (3, 1, 4) by the reference's ParamsVersion::operator<
+    (RRSPH_PARAMS/src/Version.h:17-21), which compares each component on its
+    own: major <= 3 and minor <= 1 and patch < 4 (so 3.0.5 is not older)."""
+    major, minor, patch = (int(js.get(f"params_target_version_{k}", 0)) for k in ("major", "minor", "patch"))
+    return major <= 3 and minor <= 1 and patch < 4
 
 
 def load(model: dict, particle: dict) -> OracleParams:

@@ -166,7 +166,10 @@ extern "C" int rrsph_experiment_load_params(const char* experiment_dir, rrsph_pa
             L.opt("params_target_version_major", ver[0]);
             L.opt("params_target_version_minor", ver[1]);
             L.opt("params_target_version_patch", ver[2]);
-            const bool old = ver[0] < 3 || (ver[0] == 3 && (ver[1] < 1 || (ver[1] == 1 && ver[2] < 4)));
+            // target < current (3.1.4) as the reference's ParamsVersion::operator< has it
+            // (RRSPH_PARAMS/src/Version.h:17-21): every component compared on its own
+            // (major <= 3, minor <= 1, patch < 4), not lexicographically
+            const bool old = ver[0] <= 3 && ver[1] <= 1 && ver[2] < 4;
 
             L.opt_u("density_treatment", p->density_treatment);
             uint32_t density_normalization = 0;

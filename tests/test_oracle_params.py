@@ -45,7 +45,10 @@ def _variants():
                       ("specific_c", {"eos_sound_vel_method": 1, "eos_sound_vel": 900.0}),
                       ("gauss", {"density_skf": 2, "intf_skf": 2, "artificial_viscosity_skf": 2,
                                  "average_velocity_skf": 2, "artificial_pressure_skf": 2}),
-                      ("old_version", {"params_target_version_minor": 0})):
+                      ("old_version", {"params_target_version_minor": 0, "params_target_version_patch": 0}),
+                      ("version_3_0_5", {"params_target_version_minor": 0, "params_target_version_patch": 5}),
+                      ("no_version", {"params_target_version_major": 0, "params_target_version_minor": 0,
+                                      "params_target_version_patch": 0, "nwm_direction": 0})):
         c = cases.dam_break_2d(nx=40, ny=20)
         c.model = dict(base.model, **upd)
         out.append((name, c))
@@ -91,6 +94,22 @@ def test_reference_case_loading_and_eos_sound_velocity():
         dq = OP.derive(q, None) if isinstance(q, OP.OracleParams) else derive(q, None)
         assert dq.eos_sound_vel == model["eos_sound_vel"]
     assert d.hsml == b.delta * b.intf_hsml_coef and d.maxn == 32768 and d.mass == 1000.0 * (b.delta * b.delta)
+
+
+def test_version_comparison_is_the_references():
+    """ModelParams.json older than 3.1.4 gets nwm_direction = 1
+    (backward_compatibility_model_params, ModelParams.cpp:162-167), with the
+    reference's component-wise comparison (Version.h:17-21)."""
+    from oracle import params as OP
+    from sph2d_gb300 import cases, params_from_json
+
+    c = cases.dam_break_2d(nx=10, ny=5)
+    for ver, old in (((3, 1, 4), False), ((0, 0, 0), True), ((3, 1, 3), True), ((3, 0, 5), False),
+                     ((2, 5, 0), False), ((3, 0, 0), True)):
+        m = dict(c.model, nwm_direction=0, params_target_version_major=ver[0], params_target_version_minor=ver[1],
+                 params_target_version_patch=ver[2])
+        assert OP.load(m, c.particle).nwm_direction == (1 if old else 0), ver
+        assert params_from_json(m, c.particle).nwm_direction == (1 if old else 0), ver
 
 
 def test_loading_errors_match_the_reference_messages():
