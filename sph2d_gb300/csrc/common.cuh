@@ -77,6 +77,10 @@ struct DevParams {
     // neighbour reuse (mixed step): list cutoff (cell + skin)^2, (skin / 2)^2, and
     // the distance from a cell edge within which the list looks two cells away
     float vl_cut2, vl_half_skin2, vl_skin_edge;
+    // 1: the key pass leaves the cell table of the last list build in place
+    // (the cell-tile density pass reads it on reuse steps); each rebuild then
+    // clears the table wholesale before the reorder writes the new one
+    int keep_cells;
     MixedF mf;
 };
 

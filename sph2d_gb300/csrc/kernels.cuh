@@ -124,6 +124,9 @@ void launch_verlet_reset(uint32_t* rebuild, uint32_t* gone, unsigned long long* 
 void launch_verlet_upload_check(uint32_t* rebuild, const uint32_t* gone, cudaStream_t st);
 template <int DIM>
 void launch_verlet_build(const DevParams& P, const State& S, const Sorted& G, cudaStream_t st);
+// Marks every cell-table entry empty (a kernel, so that it can sit in the
+// rebuild body of a step graph's conditional node).
+void launch_clear_cells(uint32_t* cell_start, uint32_t max_cells, cudaStream_t st);
 // The last reuse step's neighbour list (nlist / ncount) as particle ids:
 // counts[id], list[id * max_per + e]; more than max_per raises the overflow flag.
 template <int DIM>
@@ -171,6 +174,12 @@ template <int DIM>
 void launch_download_direct(const DevParams& P, const State& S, double* r, double* v, double* rho, double* p,
                             int32_t* itype, uint32_t stride, cudaStream_t st);
 
+// Compile-time variant: the cell-tile density pass of the 2D mixed step with
+// neighbour reuse (summation density, cubic kernel) instead of the
+// candidate-list pass (kernels_reuse.cu).
+#ifndef RRSPH_DENSITY_CELL_TILES
+#define RRSPH_DENSITY_CELL_TILES 0
+#endif
 constexpr int kVerletCap2 = 64;         // candidate-list entries per particle, 2D
 constexpr int kVerletCap3 = 256;        // and 3D
 inline int verlet_cap(int dim) { return dim == 3 ? kVerletCap3 : kVerletCap2; }

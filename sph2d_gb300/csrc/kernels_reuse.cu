@@ -326,6 +326,180 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density_verlet(DevParams 
     warp_sum_add(&scal->pairs, cnt);
 }
 
+#if RRSPH_DENSITY_CELL_TILES
+// The cell-tile variant of the 2D summation density pass (compile-time switch
+// RRSPH_DENSITY_CELL_TILES=1; the candidate-list pass above is the default).
+// Each warp (32 consecutive particles in the build's cell order, a 2x2 block
+// of cells or two) stages the particles of its cells' neighbourhood, the
+// bounding box of its build cells widened by two cells each way, from the
+// cell table into shared memory; each lane then tests every particle of the
+// build cells in its particle's window (the 3x3 to 4x4 cells k_vl_build
+// searched) against the reference's cutoff, with the same float test, guard
+// band and double re-test, and writes this step's neighbour list for the
+// force pass as the list variant does. A warp whose box or particle count
+// exceeds the stage reads the cell table and the particles from global memory
+// instead. The cell table read here is the one of the last list build: with
+// this variant the key pass leaves it in place (DevParams::keep_cells) and
+// each rebuild clears it wholesale.
+constexpr int kTileWarps = 4;         // warps per block
+constexpr int kTileBoxCells = 64;     // cells of a staged box
+constexpr int kTileCap = 384;         // particles of a staged box
+struct TileStage {
+    float4 p[kTileCap];
+    uint32_t start[kTileBoxCells];    // first stage index of a box cell
+    uint32_t slot0[kTileBoxCells];    // its first sorted index
+    uint32_t count[kTileBoxCells];
+};
+
+template <bool STAGED>
+__device__ __forceinline__ void tile_density_cells(const DevParams& P, const State& S, const Sorted& G,
+                                                   const TileStage& T, uint32_t k, uint32_t cx, uint32_t cy,
+                                                   uint32_t bx0, uint32_t by0, uint32_t bw, float4 pj,
+                                                   Kahan& acc, uint32_t& cnt, uint4& nb, uint4* nout) {
+    const MixedF& M = P.mf;
+    const float f = M.kf[1];
+    const float2 bo = S.boff[G.id[k]];
+    int x0, x1, y0, y1;
+    vl_window<2>(bo.x, cx, M.cell, P.vl_skin_edge, x0, x1);
+    vl_window<2>(bo.y, cy, M.cell, P.vl_skin_edge, y0, y1);
+#pragma unroll 1
+    for (int dx = x0; dx <= x1; dx++) {
+#pragma unroll 1
+        for (int dy = y0; dy <= y1; dy++) {
+            uint32_t s, c, base;
+            if (STAGED) {
+                const uint32_t b = (cx + dx - bx0) + (cy + dy - by0) * bw;
+                c = T.count[b];
+                s = T.slot0[b];
+                base = T.start[b];
+            } else {
+                const uint32_t cell = split2_32(cx + dx) | (split2_32(cy + dy) << 1);
+                if (cell >= P.max_cells) continue;
+                s = G.cell_start[cell];
+                if (s == kEmpty) continue;
+                c = G.cell_end[cell] - s;
+                base = s;
+            }
+            const float shx = (float)dx * M.cell - pj.x;
+            const float shy = (float)dy * M.cell - pj.y;
+            const uint32_t code = vl_code<2>(dx, dy, 0);
+            float part = 0.0f;
+            for (uint32_t t = 0; t < c; t++) {
+                const uint32_t i = s + t;
+                const float4 pi = STAGED ? T.p[base + t] : G.P4[base + t];
+                const float ddx = pi.x + shx, ddy = pi.y + shy;
+                const float d2 = ddx * ddx + ddy * ddy;
+                bool in = i != k && __float_as_int(pi.w) != P.type_non_existent && d2 < M.cut2_hi;
+                if (in && !(d2 < M.cut2_lo)) in = within_cutoff<2>(P, S, G, i, k, d2);
+                if (in) {
+                    const float inv_dist = rsqrtf(d2);
+                    part += cubic_wf_sel(f, d2 * inv_dist * M.inv_h);
+                    const uint32_t slot = cnt & 3u, en = i | code;
+                    nb.x = slot == 0 ? en : nb.x;
+                    nb.y = slot == 1 ? en : nb.y;
+                    nb.z = slot == 2 ? en : nb.z;
+                    nb.w = slot == 3 ? en : nb.w;
+                    if (slot == 3 && cnt < (uint32_t)kVerletCap2) nout[(size_t)(cnt >> 2) * P.n] = nb;
+                    cnt++;
+                }
+            }
+            acc.add(M.mass * part);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kTileWarps * 32) k_density_tiles(DevParams P, State S, Sorted G,
+                                                                   StepScalars* __restrict__ scal,
+                                                                   uint32_t* __restrict__ flags) {
+    asm volatile("griddepcontrol.launch_dependents;");
+    __shared__ TileStage stage[kTileWarps];
+    TileStage& T = stage[threadIdx.x >> 5];
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = k < P.n;
+    // the warp's build cells and their bounding box, two cells wider each way
+    uint32_t cx = 0, cy = 0;
+    if (active) {
+        const uint32_t key = G.key[k];
+        cx = second_bits(key);
+        cy = second_bits(key >> 1);
+    }
+    const uint32_t xmin = __reduce_min_sync(0xFFFFFFFFu, active ? cx : 0xFFFFFFFFu);
+    const uint32_t xmax = __reduce_max_sync(0xFFFFFFFFu, active ? cx : 0u);
+    const uint32_t ymin = __reduce_min_sync(0xFFFFFFFFu, active ? cy : 0xFFFFFFFFu);
+    const uint32_t ymax = __reduce_max_sync(0xFFFFFFFFu, active ? cy : 0u);
+    if (xmin == 0xFFFFFFFFu) return;  // no particle in this warp
+    const uint32_t bx0 = xmin >= 2 ? xmin - 2 : 0, by0 = ymin >= 2 ? ymin - 2 : 0;
+    const uint32_t bx1 = xmax + 2 <= kMaxCellCoord2 ? xmax + 2 : kMaxCellCoord2;
+    const uint32_t by1 = ymax + 2 <= kMaxCellCoord2 ? ymax + 2 : kMaxCellCoord2;
+    const uint32_t bw = bx1 - bx0 + 1, nbox = bw * (by1 - by0 + 1);
+    bool staged = nbox <= (uint32_t)kTileBoxCells;
+    if (staged) {
+        // per box cell: its range in the sorted order, and an exclusive prefix
+        // of the counts over the box (two rounds of 32 cells)
+        uint32_t total = 0;
+        for (uint32_t b0 = 0; b0 < nbox; b0 += 32) {
+            const uint32_t b = b0 + lane;
+            uint32_t s = 0, c = 0;
+            if (b < nbox) {
+                const uint32_t cell = split2_32(bx0 + b % bw) | (split2_32(by0 + b / bw) << 1);
+                if (cell < P.max_cells) {
+                    s = G.cell_start[cell];
+                    if (s != kEmpty) c = G.cell_end[cell] - s;
+                    else s = 0;
+                }
+            }
+            uint32_t incl = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (lane >= (uint32_t)o) incl += v;
+            }
+            if (b < nbox) {
+                T.start[b] = total + incl - c;
+                T.slot0[b] = s;
+                T.count[b] = c;
+            }
+            total += __shfl_sync(0xFFFFFFFFu, incl, 31);
+        }
+        staged = total <= (uint32_t)kTileCap;
+        __syncwarp();
+        if (staged) {
+            for (uint32_t b = lane; b < nbox; b += 32) {
+                const uint32_t s = T.slot0[b], c = T.count[b], d = T.start[b];
+                for (uint32_t t = 0; t < c; t++) T.p[d + t] = G.P4[s + t];
+            }
+        }
+        __syncwarp();
+    }
+    uint32_t cnt = 0;
+    if (active) {
+        const MixedF& M = P.mf;
+        const uint32_t id = G.id[k];
+        const float4 pj = G.P4[k];
+        Kahan acc{0.0f, 0.0f};
+        uint4* const nout = reinterpret_cast<uint4*>(G.nlist) + k;  // group g at nout[g * n]
+        uint4 nb = make_uint4(kVlNone, kVlNone, kVlNone, kVlNone);
+        if (__float_as_int(pj.w) != P.type_non_existent) {
+            if (staged) tile_density_cells<true>(P, S, G, T, k, cx, cy, bx0, by0, bw, pj, acc, cnt, nb, nout);
+            else tile_density_cells<false>(P, S, G, T, k, cx, cy, bx0, by0, bw, pj, acc, cnt, nb, nout);
+            if ((cnt & 3u) && cnt < (uint32_t)kVerletCap2) nout[(size_t)(cnt >> 2) * P.n] = nb;
+        }
+        G.ncount[k] = cnt < (uint32_t)kVerletCap2 ? cnt : (uint32_t)kVerletCap2;
+        if (cnt > P.max_nb - 1) atomicOr(flags, RRSPH_FLAG_NEIGHBOUR_OVERFLOW);
+        const float d = ((acc.s - M.rho0_minus_w0_hi) - acc.c) - M.rho0_minus_w0_lo;
+        const float rho = M.rho0 + d;
+        const float pr = eos_pf(M, d);
+        const float2 prr = make_float2(pr, pr * __frcp_rn(rho * rho));
+        reinterpret_cast<float2*>(G.V4 + k)[1] = make_float2(P.intf_form == 1 ? prr.x : prr.y, rho);
+        G.PR[k] = prr;
+        S.rho[id] = P.rho0 + f2d(d);
+        S.p[id] = f2d(pr);
+    }
+    warp_sum_add(&scal->pairs, cnt);
+}
+#endif
+
 // update_acceleration over this step's neighbours: the list the density pass
 // wrote (or the stencil search for an overflowed list). In 2D a neighbour's
 // pressure comes with its velocity and density (V4.z); in 3D from PR. STD: the
@@ -512,6 +686,13 @@ void launch_density_verlet(const DevParams& P, const State& S, const Sorted& G, 
                            cudaStream_t st, int threads) {
     const unsigned blocks = (P.n + threads - 1) / threads;
     const bool cont = P.density_treatment != 0;
+#if RRSPH_DENSITY_CELL_TILES
+    if (DIM == 2 && !cont && P.all_cubic) {
+        constexpr int tt = kTileWarps * 32;
+        k_density_tiles<<<(P.n + tt - 1) / tt, tt, 0, st>>>(P, S, G, scal, flags);
+        return;
+    }
+#endif
     if (P.all_cubic) {
         if (cont) k_density_verlet<DIM, 1, true><<<blocks, threads, 0, st>>>(P, S, G, scal, flags);
         else k_density_verlet<DIM, 1, false><<<blocks, threads, 0, st>>>(P, S, G, scal, flags);
@@ -595,6 +776,17 @@ void launch_nlist_export(const DevParams& P, const Sorted& G, uint32_t* counts, 
                          uint32_t* flags, cudaStream_t st) {
     const unsigned blocks = (P.n + 255) / 256;
     k_nlist_export<DIM><<<blocks, 256, 0, st>>>(P, G, counts, list, max_per, flags);
+}
+
+namespace {
+__global__ void k_clear_cells(uint32_t* __restrict__ cell_start, uint32_t max_cells) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < max_cells) cell_start[c] = kEmpty;
+}
+}  // namespace
+
+void launch_clear_cells(uint32_t* cell_start, uint32_t max_cells, cudaStream_t st) {
+    k_clear_cells<<<(max_cells + 255) / 256, 256, 0, st>>>(cell_start, max_cells);
 }
 
 template void launch_nlist_export<2>(const DevParams&, const Sorted&, uint32_t*, uint32_t*, uint32_t, uint32_t*,

@@ -254,8 +254,28 @@ void set_verlet_copies(rrsph_solver* s, int read, int write) {
     }
 }
 
+// Whether the cell-tile density pass runs (compile-time variant: 2D summation
+// density with the cubic kernel), which reads the last build's cell table.
+bool tiles_active(const rrsph_solver* s) {
+    return RRSPH_DENSITY_CELL_TILES && s->verlet && s->dim == 2 && s->P.density_treatment == 0 && s->P.all_cubic;
+}
+// The key pass keeps or clears cell-table entries as the density pass needs;
+// on a change the table is cleared wholesale (no entry of another grid stays).
+int set_keep_cells(rrsph_solver* s) {
+    const int keep = tiles_active(s) ? 1 : 0;
+    if (keep != s->P.keep_cells) {
+        s->P.keep_cells = keep;
+        RRSPH_CUDA_TRY(cudaMemsetAsync(s->G.cell_start, 0xFF, (size_t)s->P.max_cells * sizeof(uint32_t), s->stream));
+    }
+    return RRSPH_OK;
+}
+
 void enqueue_verlet_rebuild(rrsph_solver* s, cudaStream_t st) {
     rrsph::launch_verlet_reset(s->S.vl_rebuild, s->S.vl_gone, s->vl_builds, st);
+    if (s->P.keep_cells) {  // the previous build's table stayed in place: clear it for the reorder
+        rrsph::launch_clear_cells(s->G.cell_start, s->P.max_cells, st);
+        s->launches++;
+    }
     rrsph::radix_sort_pairs_into(s->G.keys_in, s->G.ids_in, s->G.keys_a, s->G.ids_a, s->G.keys_b, s->G.ids_b,
                                  s->G.sort_scratch, s->P.n, s->sort_bits, st, &s->launches);
     s->G.key = s->G.keys_a;
@@ -544,6 +564,7 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
         }
         s->verlet = true;
         set_verlet_params(s);
+        s->P.keep_cells = tiles_active(s) ? 1 : 0;  // the table is cleared wholesale below
     }
     if (cudaMallocHost(&s->h_scal, sizeof(rrsph::StepScalars)) != cudaSuccess ||
         cudaMallocHost(&s->h_flags, sizeof(uint32_t)) != cudaSuccess ||
@@ -895,6 +916,8 @@ template <int DIM>
 void enqueue_component_grid(rrsph_solver* s, bool with_p) {
     s->keys_ready = false;  // this grid's keys were made without the predictor
     s->nlist_valid = false;  // and it replaces the grid the last step's list refers to
+    if (s->P.keep_cells)     // the last build's table is still in place
+        cudaMemsetAsync(s->G.cell_start, 0xFF, (size_t)s->P.max_cells * sizeof(uint32_t), s->stream);
     if (s->S.vl_rebuild) cudaMemsetAsync(s->S.vl_rebuild, 0xFF, sizeof(uint32_t), s->stream);
     rrsph::GatherSrc fsrc{s->S.vx, s->S.vy, s->S.vz, s->S.rho, with_p ? s->S.p : nullptr, 0};
     enqueue_grid<DIM>(s, 0, s->scal, fsrc);
@@ -1101,7 +1124,7 @@ extern "C" int rrsph_kernel_launches(rrsph_solver* s, uint64_t* launches) {
         int rc = rrsph_neighbour_rebuilds(s, &builds);
         if (rc) return rc;
     }
-    *launches = s->launches + builds * s->vl_extra_launches;
+    *launches = s->launches + builds * (s->vl_extra_launches + (s->P.keep_cells ? 1ull : 0ull));
     return RRSPH_OK;
 }
 
@@ -1133,6 +1156,7 @@ extern "C" int rrsph_set_neighbour_reuse(rrsph_solver* s, int enable, double ski
         s->verlet_skin = skin_over_h;
         set_verlet_params(s);
     }
+    if ((rc = set_keep_cells(s)) != 0) return rc;
     if (s->S.vl_rebuild) RRSPH_CUDA_TRY(cudaMemsetAsync(s->S.vl_rebuild, 0xFF, sizeof(uint32_t), s->stream));
     s->keys_ready = false;
     return RRSPH_OK;

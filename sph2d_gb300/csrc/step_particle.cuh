@@ -91,7 +91,7 @@ __device__ __forceinline__ void key_pass(const DevParams& P, const State& S, con
         if (key >= P.max_cells) key = P.max_cells - 1;
     }
     const uint32_t old = S.key_of[i];
-    if (old < P.max_cells) G.cell_start[old] = kEmpty;
+    if (old < P.max_cells && !P.keep_cells) G.cell_start[old] = kEmpty;
     S.key_of[i] = (uint32_t)key;
     G.keys_in[i] = (uint32_t)key;
     G.ids_in[i] = i;
