@@ -40,7 +40,9 @@ def gauges(r: np.ndarray, itype: np.ndarray, xs, radius: float) -> np.ndarray:
     return out
 
 
-def run_gpu(p, case, precision: str, steps: int, every: int, xs, radius: float):
+def run_gpu(p, case, precision: str, steps: int, every: int, xs, radius: float, stats: dict | None = None):
+    """Gauge series of a GPU run sampled every `every` steps; `stats` (if
+    given) receives the directed pairs summed over the run."""
     from sph2d_gb300 import Solver
 
     series = []
@@ -58,6 +60,8 @@ def run_gpu(p, case, precision: str, steps: int, every: int, xs, radius: float):
             st = s.download()
             series.append((done, t, gauges(st["r"], st["itype"], xs, radius)))
         wall = time.perf_counter() - t0
+        if stats is not None:
+            stats["pairs_total"] = s.pair_count()[1]
     return series, wall
 
 
