@@ -87,8 +87,9 @@ def workload_config(case, pairs_first: int, warmup: int, steps: int) -> dict:
 
 GPU_METHOD = {
     "precision": "mixed (f32 pairs, f64 state/integration)",
-    "neighbour_search": "candidate lists within cutoff + 0.3 h, rebuilt when a particle has moved 0.15 h",
-    "l2": "flushed (256 MiB device write) before every timed step",
+    "neighbour_search": "candidate lists within cutoff + 0.5 h, rebuilt when a particle has moved 0.25 h",
+    "l2": "not flushed: the timed steps run back to back as the time loop runs them; one step reads and "
+          "writes ~160 MB of particle state and neighbour lists (> 129 MB L2)",
 }
 
 
@@ -179,9 +180,10 @@ def _time_steps(solver, flush, steps: int) -> float:
 
 
 def _loop_ms(solver, steps: int) -> float:
-    """Device milliseconds per step of `steps` steps back to back, as a
-    simulation loop runs them (no flush: each step reads what the last one
-    wrote, and the per-step working set is larger than the L2)."""
+    """Device milliseconds per step of `steps` steps back to back (one graph
+    launch each) between two CUDA events on the solver's stream, as the time
+    loop runs them: no flush between steps, whose per-step data (~160 MB of
+    particle state and neighbour lists on the flume) exceed the 129 MB L2."""
     import torch
 
     ext = torch.cuda.ExternalStream(solver.stream)
@@ -195,15 +197,18 @@ def _loop_ms(solver, steps: int) -> float:
 
 
 def _phase_pass(solver, flush, steps: int):
-    """Per-phase milliseconds per step (events between the kernels of each phase)."""
+    """Per-phase milliseconds per step (events between the kernels of each
+    phase; direct launches). flush: a tensor written before every step (the
+    L2 flushed), or None (steps back to back)."""
     import torch
 
     ext = torch.cuda.ExternalStream(solver.stream)
     solver.set_phase_timing(True)
     solver.phase_times(reset=True)
     for _ in range(steps):
-        with torch.cuda.stream(ext):
-            flush.add_(1)
+        if flush is not None:
+            with torch.cuda.stream(ext):
+                flush.add_(1)
         solver.step_async(1)
     solver.sync()
     times, n = solver.phase_times(reset=True)
@@ -255,9 +260,11 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    # clocks sampled from the start of the timed steps to the end of the e2e
+    # loop (the K timed steps alone last ~K x 0.12 ms, shorter than the
+    # sampling interval)
     clocks.start()
-    ms_mixed = _time_steps(sm, flush, args.steps)
-    clocks_info = clocks.stop()
+    ms_mixed = _loop_ms(sm, args.steps) * args.steps
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -265,9 +272,13 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     rebuilds = sm.neighbour_rebuilds() - rebuilds0
     diag1 = sm.diagnostics()
     last_pairs, pairs1 = sm.pair_count()
-    loop_ms = _loop_ms(sm, args.steps)
     pairs_timed = pairs1 - pairs0
-    phases_mixed = _phase_pass(sm, flush, min(args.steps, 50))
+    # the same step, each after a 256 MiB write that flushes the L2 (stated beside)
+    flushed_steps = min(args.steps, 50)
+    _, f0 = sm.pair_count()
+    flushed_ms = _time_steps(sm, flush, flushed_steps)
+    _, f1 = sm.pair_count()
+    phases_mixed = _phase_pass(sm, None, min(args.steps, 50))
 
     # ---- FP64 step beside it
     steps64 = max(3, min(args.steps, 30))
@@ -277,9 +288,9 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     s64.step_async(max(2, min(args.warmup, 3)))
     s64.sync()
     _, q0 = s64.pair_count()
-    ms_fp64 = _time_steps(s64, flush, steps64)
+    ms_fp64 = _loop_ms(s64, steps64) * steps64
     _, q1 = s64.pair_count()
-    phases_fp64 = _phase_pass(s64, flush, min(steps64, 10))
+    phases_fp64 = _phase_pass(s64, None, min(steps64, 10))
 
     # ---- error of the mixed step against the FP64 GPU step (same start, same
     # steps), every field the step writes: state r, v, rho, p and the rates a
@@ -331,19 +342,25 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
                                     ip(host["itype"])))
         return sm.pair_count()[0]
 
-    # as many steps as the timed device loop, at most 200: one stall of the
-    # host weighs little in the mean
-    e2e_steps = max(5, min(args.steps, 200))
+    # 200 steps whatever K is (~85 ms): a stall of the host (the GPU machine's
+    # cores are shared with other work) weighs little in the mean
+    e2e_steps = 200
     for _ in range(max(3, args.warmup)):
         e2e_step()
     rb0 = sm.neighbour_rebuilds()
     torch.cuda.synchronize()
     e2e_pairs = 0
+    e2e_each = []
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
+        ts = time.perf_counter()
         e2e_pairs += e2e_step()
+        e2e_each.append(time.perf_counter() - ts)
     e2e_s = time.perf_counter() - t0
     e2e_rebuilds = sm.neighbour_rebuilds() - rb0
+    clocks_info = clocks.stop()
+    if clocks_info is not None:
+        clocks_info["window"] = "from the timed steps to the end of the e2e loop"
     h2d = n * (2 * 8 + 2 * 8 + 8 + 8 + 4)
     d2h = n * (2 * 8 + 2 * 8 + 8 + 8 + 4)
 
@@ -375,8 +392,10 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         "steps": args.steps,
         "warmup": args.warmup,
         "ms_per_step": ms_mixed / args.steps,
-        "steady_loop": {"ms_per_step": loop_ms, "steps": args.steps,
-                        "note": "the same step back to back without the L2 flush (per-step working set ~200 MB > L2)"},
+        "l2_flushed": {"ms_per_step": flushed_ms / flushed_steps, "steps": flushed_steps,
+                       "pair_interactions_per_s": (f1 - f0) / (flushed_ms / 1e3),
+                       "note": "the steps after the timed ones, each after a 256 MiB device write that flushes the "
+                               "L2, timed one step per pair of CUDA events"},
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
@@ -427,6 +446,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         },
         "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": e2e_steps, "rebuilds": e2e_rebuilds,
+                "ms_per_step_median": statistics.median(e2e_each) * 1e3, "ms_per_step_max": max(e2e_each) * 1e3,
                 "path": "rrsph_upload + rrsph_step(1) + rrsph_download per step on pinned host buffers, each "
                         "step uploading the state the last one downloaded"},
         "gpu_launches": launches,
@@ -438,7 +458,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
             "note": "rrsph_diagnostics_get before and after the timed steps (double, fixed-order sums)",
         },
         "neighbour_rebuilds": {"timed_steps": args.steps, "rebuilds": rebuilds,
-                               "note": "grid + candidate lists rebuilt when a particle moved half the 0.3 h skin"},
+                               "note": "grid + candidate lists rebuilt when a particle moved half the 0.5 h skin"},
         "clocks": clocks_info,
     }
     sm.close()
@@ -460,9 +480,9 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
 
 def ensemble_measure(steps: int = 50, seq_steps: int = 10, ntanks: int = 256) -> dict:
     """Batched ensemble: every tank packed into one mixed-precision solver (one
-    graph launch per step for all tanks, gather block sizes from the
-    autotuner) against the same tanks stepped one after another, each in its
-    own solver."""
+    graph launch per step for all tanks, gather block sizes and the candidate
+    lists' skin from the autotuners) against the same tanks stepped one after
+    another, each in its own solver."""
     import torch
 
     from sph2d_gb300 import Solver, cases
@@ -477,6 +497,7 @@ def ensemble_measure(steps: int = 50, seq_steps: int = 10, ntanks: int = 256) ->
         s.step_async(3)
         s.sync()
         threads = s.autotune(steps=3)
+        skin = s.autotune_skin(steps=30)
         s.step_async(3)
         s.sync()
         _, q0 = s.pair_count()
@@ -516,7 +537,7 @@ def ensemble_measure(steps: int = 50, seq_steps: int = 10, ntanks: int = 256) ->
                     "period 1-2 s (seed 5); FP32-mixed step",
         "tanks": ntanks, "particles": ens.ntotal, "fluid_particles": int(ens.notes["nfluid"]),
         "batched": {"ms_per_step": ms / steps, "pair_interactions_per_s": batched_rate, "steps": steps,
-                    "gather_threads": {"density": threads[0], "forces": threads[1]}},
+                    "gather_threads": {"density": threads[0], "forces": threads[1]}, "skin_over_h": skin},
         "sequential": {"ms_per_step": seq_ms, "pair_interactions_per_s": seq_rate, "steps_per_tank": seq_steps},
         "speedup": seq_ms / (ms / steps),
         "launches_in_batched_region": launches,

@@ -399,6 +399,14 @@ int rrsph_set_gather_threads(rrsph_solver* s, uint32_t density_threads, uint32_t
  * candidate gather block sizes (64, 128, 256), keeps the fastest and puts the
  * state back. threads_out[2] (may be NULL) receives {density, forces}. */
 int rrsph_autotune(rrsph_solver* s, uint32_t steps, uint32_t* threads_out);
+/* Autotuner of the candidate lists' skin (the FP32-mixed step with neighbour
+ * reuse): for skins of 0.2, 0.3, 0.4, 0.5, 0.6 and 0.8 hsml in turn, rebuilds
+ * the grid and lists of the uploaded state, runs two untimed steps, times
+ * `steps` steps (with the rebuilds that skin asks for) and puts the state
+ * back; keeps the fastest skin, and the next step rebuilds. A trial of a few
+ * tens of steps weighs the rebuild frequency. skin_out (may be NULL)
+ * receives the skin in hsml. RRSPH_ERR_UNSUPPORTED for other solvers. */
+int rrsph_autotune_skin(rrsph_solver* s, uint32_t steps, double* skin_out);
 
 /* Neighbour reuse of the FP32-mixed step, 2D or 3D, summation or continuity
  * density (on by default there): each particle's candidate list holds the particles within
@@ -406,7 +414,9 @@ int rrsph_autotune(rrsph_solver* s, uint32_t steps, uint32_t* threads_out);
  * grid and lists are rebuilt only when a particle has moved more than half the
  * skin since then, so every pair within the cutoff stays in the lists. Each
  * step still applies the reference's cutoff test to the list: the pairs are
- * the reference's. RRSPH_ERR_UNSUPPORTED for other solvers. */
+ * the reference's. The skin defaults to 0.5 hsml in 2D and 0.3 hsml in 3D;
+ * skin_over_h = 0 keeps the current one. Every call makes the next step
+ * rebuild the grid and the lists. RRSPH_ERR_UNSUPPORTED for other solvers. */
 int rrsph_set_neighbour_reuse(rrsph_solver* s, int enable, double skin_over_h);
 /* Grid + list rebuilds since the solver was created (0 without reuse). */
 int rrsph_neighbour_rebuilds(rrsph_solver* s, uint64_t* rebuilds);

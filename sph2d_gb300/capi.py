@@ -199,6 +199,7 @@ _SIGS = {
     "rrsph_set_wave_makers": (C.c_int, [C.c_void_p, C.c_uint32, _P(RrsphWaveMaker)]),
     "rrsph_set_gather_threads": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
     "rrsph_autotune": (C.c_int, [C.c_void_p, C.c_uint32, _u32p]),
+    "rrsph_autotune_skin": (C.c_int, [C.c_void_p, C.c_uint32, _P(C.c_double)]),
     "rrsph_set_neighbour_reuse": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "rrsph_neighbour_rebuilds": (C.c_int, [C.c_void_p, _P(C.c_uint64)]),
 }

@@ -563,6 +563,7 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
                                                           " failed: " + cudaGetErrorString(e)));
         }
         s->verlet = true;
+        s->verlet_skin = s->dim == 3 ? kDefaultSkin3 : kDefaultSkin2;
         set_verlet_params(s);
         s->P.keep_cells = tiles_active(s) ? 1 : 0;  // the table is cleared wholesale below
     }
@@ -1147,8 +1148,9 @@ extern "C" int rrsph_set_neighbour_reuse(rrsph_solver* s, int enable, double ski
     if (enable && !s->S.vl_rebuild)
         return set_error(RRSPH_ERR_UNSUPPORTED, "neighbour reuse needs an FP32-mixed solver (at most 2^27 particles "
                                                 "in 2D, 2^25 in 3D)");
-    if (enable && !(skin_over_h > 0 && skin_over_h <= 1))
-        return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_set_neighbour_reuse: skin must be in (0, 1] hsml");
+    if (enable && !(skin_over_h >= 0 && skin_over_h <= 1))
+        return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_set_neighbour_reuse: skin must be in (0, 1] hsml, or 0");
+    if (skin_over_h == 0) skin_over_h = s->verlet_skin;  // keep the current skin
     drop_graphs(s);
     s->verlet = enable != 0;
     s->nlist_valid = false;
@@ -1317,6 +1319,66 @@ extern "C" int rrsph_autotune(rrsph_solver* s, uint32_t steps, uint32_t* threads
         threads_out[1] = (uint32_t)best_f;
     }
     // flags the trial steps raised belong to no step the caller ran
+    RRSPH_CUDA_TRY(cudaMemcpy(s->flags, &flags_before, sizeof(uint32_t), cudaMemcpyHostToDevice));
+    return RRSPH_OK;
+}
+
+extern "C" int rrsph_autotune_skin(rrsph_solver* s, uint32_t steps, double* skin_out) {
+    int rc = check_handle(s, "rrsph_autotune_skin");
+    if (rc) return rc;
+    if (steps == 0) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_autotune_skin: steps must be positive");
+    if (!s->verlet) return set_error(RRSPH_ERR_UNSUPPORTED, "rrsph_autotune_skin: needs the mixed step with neighbour reuse");
+    uint32_t flags_before = 0;
+    RRSPH_CUDA_TRY(cudaMemcpy(&flags_before, s->flags, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    Backup b;
+    if ((rc = backup_state(s, b)) != 0) {
+        if (b.buf) cudaFree(b.buf);
+        return rc;
+    }
+    // each trial starts from a fresh build of the same state (two untimed
+    // steps, which also capture the step graphs) and times `steps` steps with
+    // the rebuilds its skin asks for: a wider skin rebuilds less often and
+    // tests more candidates per step
+    const double cand[] = {0.2, 0.3, 0.4, 0.5, 0.6, 0.8};
+    const double current = s->verlet_skin;
+    double best_skin = current;
+    float best = 0;
+    cudaEvent_t e0 = s->ev[0], e1 = s->ev[1];
+    const bool timing = s->timing;
+    s->timing = false;
+    for (double skin : cand) {
+        drop_graphs(s);
+        s->verlet_skin = skin;
+        set_verlet_params(s);
+        if (cudaMemsetAsync(s->S.vl_rebuild, 0xFF, sizeof(uint32_t), s->stream) != cudaSuccess) {
+            rc = set_error(RRSPH_ERR_CUDA, "rrsph_autotune_skin: memset");
+            break;
+        }
+        rc = enqueue_steps(s, 2);
+        if (!rc) {
+            cudaEventRecord(e0, s->stream);
+            rc = enqueue_steps(s, steps);
+            cudaEventRecord(e1, s->stream);
+        }
+        if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = set_error(RRSPH_ERR_CUDA, "rrsph_autotune_skin: event");
+        float ms = 0;
+        if (!rc) cudaEventElapsedTime(&ms, e0, e1);
+        if (!rc) rc = restore_state(s, b);
+        if (rc) break;
+        if (best == 0 || ms < best) {
+            best = ms;
+            best_skin = skin;
+        }
+    }
+    s->timing = timing;
+    cudaFree(b.buf);
+    drop_graphs(s);
+    s->verlet_skin = rc ? current : best_skin;
+    set_verlet_params(s);
+    s->nlist_valid = false;
+    RRSPH_CUDA_TRY(cudaMemsetAsync(s->S.vl_rebuild, 0xFF, sizeof(uint32_t), s->stream));
+    if (rc) return rc;
+    if (skin_out) *skin_out = best_skin;
     RRSPH_CUDA_TRY(cudaMemcpy(s->flags, &flags_before, sizeof(uint32_t), cudaMemcpyHostToDevice));
     return RRSPH_OK;
 }

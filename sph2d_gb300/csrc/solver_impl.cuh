@@ -10,6 +10,14 @@ namespace rrsph_impl {
 constexpr int kPhases = 6;
 inline const char* const kPhaseNames[kPhases] = {"keys", "sort", "reorder", "density", "forces", "whole"};
 constexpr uint32_t kFlagNeverEnding = RRSPH_FLAG_NEVER_ENDING;
+// Default skins of the candidate lists, in units of hsml. In 2D a wider skin
+// rebuilds less often for a few more candidates per particle: on the 409k
+// flume 0.5 h gave 0.1235 ms per step over 200 steps (8 rebuilds) against
+// 0.1280 ms at 0.3 h (15 rebuilds), and 0.138 against 0.160 ms over steps
+// 6-25 (3 against 6 rebuilds); 0.3 h in 3D, where the candidate count grows
+// with the cube of the radius.
+constexpr double kDefaultSkin2 = 0.5;
+constexpr double kDefaultSkin3 = 0.3;
 
 struct AdjointRun;  // a forward run recorded for the reverse sweep (adjoint.cu)
 
@@ -18,6 +26,8 @@ struct AdjointRun;  // a forward run recorded for the reverse sweep (adjoint.cu)
 using rrsph_impl::kPhases;
 using rrsph_impl::kPhaseNames;
 using rrsph_impl::kFlagNeverEnding;
+using rrsph_impl::kDefaultSkin2;
+using rrsph_impl::kDefaultSkin3;
 
 struct rrsph_solver {
     rrsph_params params{};
@@ -53,7 +63,7 @@ struct rrsph_solver {
     int gather_threads[2] = {rrsph::kGatherThreads, rrsph::kGatherThreads};  // density, forces block sizes
     // neighbour reuse of the FP32-mixed step
     bool verlet = false;
-    double verlet_skin = 0.3;                  // skin, in units of hsml
+    double verlet_skin = kDefaultSkin3;        // skin, in units of hsml (set at creation by dimension)
     cudaStream_t aux = nullptr;                // captures the rebuild / reuse bodies of a step graph
     unsigned long long* vl_builds = nullptr;   // device: list builds since creation
     uint32_t* h_vl = nullptr;                  // pinned: the rebuild flag, read with direct launches

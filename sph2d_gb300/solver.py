@@ -257,8 +257,17 @@ class Solver:
         check(lib().rrsph_autotune(self._h, steps, out))
         return int(out[0]), int(out[1])
 
-    def set_neighbour_reuse(self, enable: bool, skin_over_h: float = 0.3) -> None:
-        """Candidate-list reuse of the FP32-mixed step (2D or 3D, summation or continuity density)."""
+    def autotune_skin(self, steps: int = 30) -> float:
+        """Picks the candidate lists' skin by timing `steps` steps per
+        candidate (rebuilds included); returns it in units of hsml."""
+        v = C.c_double()
+        check(lib().rrsph_autotune_skin(self._h, steps, C.byref(v)))
+        return float(v.value)
+
+    def set_neighbour_reuse(self, enable: bool, skin_over_h: float = 0.0) -> None:
+        """Candidate-list reuse of the FP32-mixed step (2D or 3D, summation or
+        continuity density); skin_over_h 0 keeps the current skin (0.5 h in 2D,
+        0.3 h in 3D by default). The next step rebuilds the grid and lists."""
         check(lib().rrsph_set_neighbour_reuse(self._h, 1 if enable else 0, float(skin_over_h)))
 
     def neighbour_rebuilds(self) -> int:

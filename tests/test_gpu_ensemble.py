@@ -122,3 +122,45 @@ def test_autotune_keeps_the_state_and_the_results(gpu_available, precision):
             assert np.array_equal(tuned[k], plain[k]), k
         else:
             assert rel_l2(tuned[k], plain[k]) < 1e-6, k
+
+
+def test_autotune_skin_keeps_the_state(gpu_available):
+    """rrsph_autotune_skin times skins of 0.2-0.8 h on the uploaded state, puts
+    the state back and keeps the fastest; the steps after it equal a run with
+    that skin set directly (the pair counts exactly, the state to float
+    rounding)."""
+    from sph2d_gb300 import RrsphError, Solver, capi, cases
+
+    c = cases.dam_break_2d(nx=60, ny=30)
+    p = c.params()
+    with Solver(p, "mixed") as s:
+        s.upload(c.r, c.v, c.rho, c.itype)
+        t = s.step(3, 0.0)
+        before = s.download()
+        skin = s.autotune_skin(steps=12)
+        assert skin in (0.2, 0.3, 0.4, 0.5, 0.6, 0.8)
+        after = s.download()
+        for k in ("r", "v", "rho", "p", "itype"):
+            assert np.array_equal(before[k], after[k]), k
+        tuned_pairs = []
+        for _ in range(8):
+            t = s.step(1, t)
+            tuned_pairs.append(s.pair_count()[0])
+        tuned = s.download()
+    with Solver(p, "mixed") as s:
+        s.upload(c.r, c.v, c.rho, c.itype)
+        t = s.step(3, 0.0)
+        s.set_neighbour_reuse(True, skin)
+        plain_pairs = []
+        for _ in range(8):
+            t = s.step(1, t)
+            plain_pairs.append(s.pair_count()[0])
+        plain = s.download()
+    assert tuned_pairs == plain_pairs
+    for k in ("r", "v", "rho"):
+        assert rel_l2(tuned[k], plain[k]) < 1e-6, k
+    with Solver(p, "fp64") as s:
+        s.upload(c.r, c.v, c.rho, c.itype)
+        with pytest.raises(RrsphError) as e:
+            s.autotune_skin(steps=2)
+        assert e.value.code == capi.ERR_UNSUPPORTED

@@ -12,7 +12,8 @@ find_neighbours on the same double positions (the pair sets must be
 bit-exact), and the step's pair count with the oracle's:
 
 - right after upload (the first step builds the lists);
-- on a step that reuses lists built several steps earlier;
+- on every step of the next few, which reuse lists built several steps
+  earlier or rebuild them as the motion asks;
 - on the step after a forced rebuild;
 - for the full 409k-particle flume, the full 2D dam break (summation and
   continuity density), a small 3D dam break, and particles whose candidate
@@ -52,22 +53,31 @@ def _check_step_pairs(s, p, r, itype, what):
     return tot
 
 
-def _run_checks(case, p, steps_between: int = 6):
-    """Upload, the first step, reuse steps, a forced rebuild; checks the pairs of
-    each (positions from a download: the state the next step's pairs come from)."""
+def _run_checks(case, p, steps: int = 8):
+    """Upload, the first step, then `steps` steps one at a time (reuse steps,
+    whose lists are several steps old, and the rebuilds the motion asks for),
+    a forced rebuild and two steps after it; checks the pairs of each
+    (positions from a download: the state the next step's pairs come from).
+    Returns the ages, in steps, of the lists that the checked reuse steps used."""
     from sph2d_gb300 import Solver
 
+    reuse_ages = []
     with Solver(p, "mixed") as s:
         s.upload(case.r, case.v, case.rho, case.itype)
         t = s.step(1, 0.0)
         _check_step_pairs(s, p, case.r, case.itype, "first step")
         assert s.neighbour_rebuilds() == 1
-        t = s.step(steps_between, t)
-        st = s.download()
-        b0 = s.neighbour_rebuilds()
-        t = s.step(1, t)
-        reused = s.neighbour_rebuilds() == b0
-        _check_step_pairs(s, p, st["r"], st["itype"], "reuse step" if reused else "step with rebuild")
+        age = 1
+        for _ in range(steps):
+            st = s.download()
+            b0 = s.neighbour_rebuilds()
+            t = s.step(1, t)
+            reused = s.neighbour_rebuilds() == b0
+            age = age + 1 if reused else 1
+            if reused:
+                reuse_ages.append(age)
+            _check_step_pairs(s, p, st["r"], st["itype"], f"reuse step (lists {age} steps old)" if reused
+                              else "step with rebuild")
         st = s.download()
         s.set_neighbour_reuse(True)  # forces a rebuild on the next step
         b0 = s.neighbour_rebuilds()
@@ -79,7 +89,7 @@ def _run_checks(case, p, steps_between: int = 6):
             st = s.download()
             t = s.step(1, t)
             _check_step_pairs(s, p, st["r"], st["itype"], "after rebuild")
-        return reused
+        return reuse_ages
 
 
 def test_flume_full_size_step_pairs(gpu_available):
@@ -88,8 +98,8 @@ def test_flume_full_size_step_pairs(gpu_available):
 
     case = cases.piston_flume_2d()
     p = case.params()
-    reused = _run_checks(case, p, steps_between=6)
-    assert reused  # the flume keeps its lists over these steps
+    ages = _run_checks(case, p, steps=8)
+    assert ages and max(ages) >= 3, ages  # lists several steps old were checked
 
 
 @pytest.mark.parametrize("treatment", [0, 1, 2])
@@ -101,7 +111,7 @@ def test_dam_break_full_size_step_pairs(gpu_available, treatment):
     if treatment == 2:
         p.density_treatment = 2
         p.density_delta_sph_coef = 0.1
-    _run_checks(case, p, steps_between=6)
+    _run_checks(case, p, steps=6)
 
 
 @pytest.mark.parametrize("treatment", [0, 1])
@@ -111,7 +121,7 @@ def test_dam_break_3d_step_pairs(gpu_available, treatment):
     case = cases.dam_break_3d(dx=0.02, tank=(0.5, 0.2, 0.3), block=(0.2, 0.2, 0.15), max_neighbours=400,
                               density_treatment=treatment)
     p = case.params()
-    _run_checks(case, p, steps_between=4)
+    _run_checks(case, p, steps=4)
 
 
 @pytest.mark.parametrize("dim", [2, 3])
