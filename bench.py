@@ -333,7 +333,8 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     e2e_time = [0.0]
 
     def e2e_step():
-        capi.check(L.rrsph_upload(sm.handle, dp(host["r"]), 2, dp(host["v"]), dp(host["rho"]), dp(host["p"]),
+        # p is not an input of the step (the density pass computes it from rho), as in the reference's loop
+        capi.check(L.rrsph_upload(sm.handle, dp(host["r"]), 2, dp(host["v"]), dp(host["rho"]), None,
                                   ip(host["itype"])))
         tt = C.c_double(e2e_time[0])
         capi.check(L.rrsph_step(sm.handle, 1, C.byref(tt)))
@@ -361,8 +362,8 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     clocks_info = clocks.stop()
     if clocks_info is not None:
         clocks_info["window"] = "from the timed steps to the end of the e2e loop"
-    h2d = n * (2 * 8 + 2 * 8 + 8 + 8 + 4)
-    d2h = n * (2 * 8 + 2 * 8 + 8 + 8 + 4)
+    h2d = n * (2 * 8 + 2 * 8 + 8 + 4)      # r, v, rho, itype
+    d2h = n * (2 * 8 + 2 * 8 + 8 + 8 + 4)  # r, v, rho, p, itype
 
     # ---- aggregate over ranks (max time, summed pairs)
     t_s = ms_mixed / 1e3

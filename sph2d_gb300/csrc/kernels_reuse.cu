@@ -89,6 +89,12 @@ __device__ __forceinline__ void vl_window(float p, uint32_t c, float cell, float
     hi = (p > cell - edge && c + 2 <= Vl<DIM>::cmax) ? 2 : (c + 1 <= Vl<DIM>::cmax ? 1 : 0);
 }
 
+// Distance along one axis from a particle at offset p in [0, cell] from its
+// cell's lower edge to the nearest side of the cell d cells away.
+__device__ __forceinline__ float gap_to_cell(int d, float p, float cell) {
+    return d > 0 ? (float)d * cell - p : (d < 0 ? p - (float)(d + 1) * cell : 0.0f);
+}
+
 // After this step's grid (sort + reorder): each particle's candidates, four
 // entries gathered in registers and stored as one uint4 into the group's slab
 // (the lanes of a warp store neighbouring uint4s), in cell order x outer.
@@ -130,6 +136,13 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_vl_build(DevParams P, Sta
             for (int dy = y0; dy <= y1; dy++) {
 #pragma unroll 1
                 for (int dz = z0; dz <= z1; dz++) {
+                    // a cell none of whose points lies within the list cutoff of the
+                    // particle holds no candidate: the distance from the particle
+                    // to the cell's nearest side, per axis (the window's corner and
+                    // far diagonal cells mostly)
+                    const float gx = gap_to_cell(dx, pj.x, M.cell), gy = gap_to_cell(dy, pj.y, M.cell);
+                    const float gz = DIM == 3 ? gap_to_cell(dz, pj.z, M.cell) : 0.0f;
+                    if (gx * gx + gy * gy + gz * gz >= P.vl_cut2) continue;
                     const uint32_t cell = DIM == 3 ? split3_32(cx + dx) | (split3_32(cy + dy) << 1) |
                                                          (split3_32(cz + dz) << 2)
                                                    : split2_32(cx + dx) | (split2_32(cy + dy) << 1);
