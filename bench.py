@@ -221,6 +221,22 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b)) / (nb if nb > 0 else 1.0)
 
 
+def aggregate_replicas(t_s: float, pairs: float, e2e_s: float, e2e_pairs: float, dist=None, device="cpu"):
+    """Whole-job figures of N independent replicas (one per rank, weak
+    scaling): the slowest rank's timed-region and e2e seconds, and the pairs
+    summed over the ranks. One all-reduce of two doubles each way; with no
+    process group (one rank) the inputs come back."""
+    if dist is None or not dist.is_initialized():
+        return t_s, float(pairs), e2e_s, float(e2e_pairs)
+    import torch
+
+    tt = torch.tensor([t_s, e2e_s], device=device, dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    pp = torch.tensor([float(pairs), float(e2e_pairs)], device=device, dtype=torch.float64)
+    dist.all_reduce(pp, op=dist.ReduceOp.SUM)
+    return float(tt[0]), float(pp[0]), float(tt[1]), float(pp[1])
+
+
 def run_gpu(args, rank: int, world: int, local_rank: int):
     import torch
 
@@ -365,18 +381,10 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     h2d = n * (2 * 8 + 2 * 8 + 8 + 4)      # r, v, rho, itype
     d2h = n * (2 * 8 + 2 * 8 + 8 + 8 + 4)  # r, v, rho, p, itype
 
-    # ---- aggregate over ranks (max time, summed pairs)
-    t_s = ms_mixed / 1e3
-    tot_pairs = pairs_timed
-    e2e_rate = e2e_pairs / e2e_s
-    if dist:
-        tt = torch.tensor([t_s, e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        pp = torch.tensor([float(pairs_timed), float(e2e_pairs)], device="cuda", dtype=torch.float64)
-        dist.all_reduce(pp, op=dist.ReduceOp.SUM)
-        t_s, e2e_max = float(tt[0]), float(tt[1])
-        tot_pairs, e2e_all = float(pp[0]), float(pp[1])
-        e2e_rate = e2e_all / e2e_max
+    # ---- aggregate over the replicas (the slowest rank's time, the pairs of all ranks)
+    t_s, tot_pairs, e2e_max, e2e_all = aggregate_replicas(ms_mixed / 1e3, pairs_timed, e2e_s, e2e_pairs, dist,
+                                                          "cuda")
+    e2e_rate = e2e_all / e2e_max
     value = tot_pairs / t_s
 
     fkey = "forces"
