@@ -154,32 +154,39 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_vl_build(DevParams P, Sta
                     const float shy = (float)dy * M.cell - pj.y;
                     const float shz = DIM == 3 ? (float)dz * M.cell - pj.z : 0.0f;
                     const uint32_t code = vl_code<DIM>(dx, dy, dz);
-                    for (uint32_t i = s; i < e; i++) {
-                        if (i == k) continue;
-                        const float4 pi = G.P4[i];
-                        if (__float_as_int(pi.w) == P.type_non_existent) continue;  // stays non-existent
-                        const float ddx = pi.x + shx, ddy = pi.y + shy, ddz = DIM == 3 ? pi.z + shz : 0.0f;
-                        const float d2 = DIM == 3 ? ddx * ddx + ddy * ddy + ddz * ddz : ddx * ddx + ddy * ddy;
-                        if (d2 < P.vl_cut2) {
-                            if (nl < (uint32_t)CAP) {
-                                const uint32_t v = i | code, slot = nl & 3u;
-                                buf.x = slot == 0 ? v : buf.x;
-                                buf.y = slot == 1 ? v : buf.y;
-                                buf.z = slot == 2 ? v : buf.z;
-                                buf.w = slot == 3 ? v : buf.w;
-                                if (slot == 3) {
-                                    slab[(size_t)(nl >> 2) * P.n] = buf;
-                                    buf = make_uint4(kVlNone, kVlNone, kVlNone, kVlNone);
+                    // the cell's particles four at a time: their loads issue together (an
+                    // index past the cell's end loads its last particle and is skipped)
+                    for (uint32_t i0 = s; i0 < e; i0 += kVlBatch) {
+                        float4 q[kVlBatch];
+#pragma unroll
+                        for (int u = 0; u < kVlBatch; u++) q[u] = G.P4[min(i0 + u, e - 1u)];
+#pragma unroll
+                        for (int u = 0; u < kVlBatch; u++) {
+                            const uint32_t i = i0 + u;
+                            // past the cell's end, itself, or non-existent (stays so): no candidate
+                            if (i >= e || i == k || __float_as_int(q[u].w) == P.type_non_existent) continue;
+                            const float ddx = q[u].x + shx, ddy = q[u].y + shy, ddz = DIM == 3 ? q[u].z + shz : 0.0f;
+                            const float d2 = DIM == 3 ? ddx * ddx + ddy * ddy + ddz * ddz : ddx * ddx + ddy * ddy;
+                            if (d2 < P.vl_cut2) {
+                                if (nl < (uint32_t)CAP) {
+                                    // shifted in: the group's entries in order once its fourth arrives
+                                    buf = make_uint4(buf.y, buf.z, buf.w, i | code);
+                                    if ((nl & 3u) == 3u) slab[(size_t)(nl >> 2) * P.n] = buf;
                                 }
+                                nl++;
                             }
-                            nl++;
                         }
                     }
                 }
             }
         }
     }
-    if (nl < (uint32_t)CAP && (nl & 3u)) slab[(size_t)(nl >> 2) * P.n] = buf;  // the padded last group
+    if (nl < (uint32_t)CAP && (nl & 3u)) {  // the padded last group: its m entries to the front
+        const uint32_t m = nl & 3u;
+        buf = m == 1u ? make_uint4(buf.w, kVlNone, kVlNone, kVlNone)
+                      : (m == 2u ? make_uint4(buf.z, buf.w, kVlNone, kVlNone) : make_uint4(buf.y, buf.z, buf.w, kVlNone));
+        slab[(size_t)(nl >> 2) * P.n] = buf;
+    }
     G.vcount[k] = nl <= (uint32_t)CAP ? nl : kListOver;
     if (nl > (uint32_t)CAP) {  // its search needs a fresh grid each step
         atomicOr(S.vl_rebuild, 1u);

@@ -182,6 +182,10 @@ void drop_graphs(rrsph_solver* s) {
         if (g) cudaGraphExecDestroy(g);
         g = nullptr;
     }
+    for (auto& g : s->graph_run) {
+        if (g) cudaGraphExecDestroy(g);
+        g = nullptr;
+    }
 }
 
 // Candidate-list cutoff (cell + skin, widened a little: a list may hold more
@@ -593,8 +597,10 @@ extern "C" void rrsph_destroy(rrsph_solver* s) {
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
     rrsph_impl::adjoint_release(s);
-    for (int i = 0; i < 2; i++)
+    for (int i = 0; i < 2; i++) {
         if (s->graph[i]) cudaGraphExecDestroy(s->graph[i]);
+        if (s->graph_run[i]) cudaGraphExecDestroy(s->graph_run[i]);
+    }
     for (int i = 0; i <= kPhases; i++)
         if (s->ev[i]) cudaEventDestroy(s->ev[i]);
     for (void* a : s->allocations)
@@ -746,12 +752,64 @@ extern "C" int rrsph_download(rrsph_solver* s, double* r, uint32_t stride, doubl
 
 namespace {
 
+// Captures `count` steps, the first of parity par0, as one executable graph.
+// A step of the reuse loop adds a conditional node whose body (the rebuild)
+// is captured after the main capture, with the step's own buffer set.
+int capture_steps(rrsph_solver* s, int par0, int count, cudaGraphExec_t* out, unsigned long long* launches_out) {
+    cudaStream_t st = s->stream;
+    cudaGraph_t g = nullptr;
+    const unsigned long long before = s->launches;
+    std::vector<std::pair<cudaGraph_t, rrsph::Sorted>> bodies;
+    RRSPH_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    int rc = RRSPH_OK;
+    for (int j = 0; j < count && rc == RRSPH_OK; j++) {
+        rc = enqueue_step_dim(s, (par0 + j) & 1, nullptr, false);
+        if (rc == RRSPH_OK && s->vl_pending) {
+            bodies.emplace_back(s->vl_body, s->G);
+            s->vl_pending = false;
+        }
+    }
+    const cudaError_t ce = cudaStreamEndCapture(st, &g);
+    if (rc == RRSPH_OK && ce != cudaSuccess)
+        rc = set_error(RRSPH_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ce));
+    const rrsph::Sorted keep = s->G;
+    for (size_t b = 0; b < bodies.size() && rc == RRSPH_OK; b++) {
+        s->G = bodies[b].second;
+        s->vl_body = bodies[b].first;
+        rc = capture_verlet_body(s);
+    }
+    s->G = keep;
+    if (rc == RRSPH_OK) {
+        const cudaError_t e = cudaGraphInstantiate(out, g, 0);
+        if (e != cudaSuccess) rc = set_error(RRSPH_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    }
+    if (g) cudaGraphDestroy(g);
+    *launches_out = s->launches - before;
+    s->launches = before;
+    return rc;
+}
+
+// The single-step graphs of both parities and the kRunSteps-step graphs
+// starting at either parity, captured together on first use.
+int ensure_graphs(rrsph_solver* s) {
+    for (int par = 0; par < 2; par++) {
+        int rc;
+        if (!s->graph[par] && (rc = capture_steps(s, par, 1, &s->graph[par], &s->launches_in_graph[par])) != 0)
+            return rc;
+        if (!s->graph_run[par] &&
+            (rc = capture_steps(s, par, kRunSteps, &s->graph_run[par], &s->launches_in_run[par])) != 0)
+            return rc;
+    }
+    return RRSPH_OK;
+}
+
 int enqueue_steps(rrsph_solver* s, uint64_t nsteps) {
     cudaStream_t st = s->stream;
-    for (uint64_t k = 0; k < nsteps; k++) {
+    for (uint64_t k = 0; k < nsteps;) {
         const int par = (int)(s->step_index & 1);
         const bool with_keys = !s->keys_ready;
         s->keys_ready = true;
+        uint64_t done = 1;
         if (s->timing) {
             int rc = enqueue_step_dim(s, par, s->ev, with_keys);
             if (rc) return rc;
@@ -763,39 +821,24 @@ int enqueue_steps(rrsph_solver* s, uint64_t nsteps) {
             }
             s->timed_steps++;
         } else if (s->graphs) {
-            if (!s->graph[par]) {
-                cudaGraph_t g = nullptr;
-                const unsigned long long before = s->launches;
-                RRSPH_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-                const int rc = enqueue_step_dim(s, par, nullptr, false);
-                const cudaError_t ce = cudaStreamEndCapture(st, &g);
-                if (rc) {
-                    if (g) cudaGraphDestroy(g);
-                    return rc;
-                }
-                if (ce != cudaSuccess)
-                    return set_error(RRSPH_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ce));
-                if (s->vl_pending) {
-                    const int rb = capture_verlet_body(s);
-                    if (rb) {
-                        cudaGraphDestroy(g);
-                        return rb;
-                    }
-                }
-                const cudaError_t e = cudaGraphInstantiate(&s->graph[par], g, 0);
-                cudaGraphDestroy(g);
-                if (e != cudaSuccess) return set_error(RRSPH_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
-                s->launches_in_graph[par] = s->launches - before;
-                s->launches = before;
-            }
+            const int rc = ensure_graphs(s);
+            if (rc) return rc;
             if (with_keys) enqueue_keys_dim(s, par);
-            RRSPH_CUDA_TRY(cudaGraphLaunch(s->graph[par], st));
-            s->launches += s->launches_in_graph[par];
+            // whole runs of kRunSteps steps as one graph launch, the rest one step each
+            if (nsteps - k >= (uint64_t)kRunSteps) {
+                RRSPH_CUDA_TRY(cudaGraphLaunch(s->graph_run[par], st));
+                s->launches += s->launches_in_run[par];
+                done = kRunSteps;
+            } else {
+                RRSPH_CUDA_TRY(cudaGraphLaunch(s->graph[par], st));
+                s->launches += s->launches_in_graph[par];
+            }
         } else {
             int rc = enqueue_step_dim(s, par, nullptr, with_keys);
             if (rc) return rc;
         }
-        s->step_index++;
+        s->step_index += done;
+        k += done;
         s->nlist_valid = s->verlet;  // the step's density pass wrote nlist on the current grid
     }
     return RRSPH_OK;

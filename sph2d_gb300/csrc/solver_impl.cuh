@@ -18,6 +18,9 @@ constexpr uint32_t kFlagNeverEnding = RRSPH_FLAG_NEVER_ENDING;
 // with the cube of the radius.
 constexpr double kDefaultSkin2 = 0.5;
 constexpr double kDefaultSkin3 = 0.3;
+// Steps per graph launch when a call asks for at least that many (even: a run
+// ends on the parity it started on); fewer run one single-step graph each.
+constexpr int kRunSteps = 10;
 
 struct AdjointRun;  // a forward run recorded for the reverse sweep (adjoint.cu)
 
@@ -28,6 +31,7 @@ using rrsph_impl::kPhaseNames;
 using rrsph_impl::kFlagNeverEnding;
 using rrsph_impl::kDefaultSkin2;
 using rrsph_impl::kDefaultSkin3;
+using rrsph_impl::kRunSteps;
 
 struct rrsph_solver {
     rrsph_params params{};
@@ -50,9 +54,11 @@ struct rrsph_solver {
     std::vector<void*> allocations;
     int sort_bits = 0;
     bool graphs = true;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};      // one step, starting at parity 0 / 1
+    cudaGraphExec_t graph_run[2] = {nullptr, nullptr};  // kRunSteps steps, starting at parity 0 / 1
     unsigned long long launches = 0;
     unsigned long long launches_in_graph[2] = {0, 0};
+    unsigned long long launches_in_run[2] = {0, 0};
     uint64_t step_index = 0;
     bool keys_ready = false;  // the next step's predict + keys were computed by the last whole step
     bool timing = false;

@@ -630,6 +630,31 @@ def test_neighbour_reuse_graph_and_direct_launches_agree(gpu_available):
         assert np.array_equal(out[0][0][k], out[1][0][k]), k
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+def test_multi_step_graphs_equal_single_steps(gpu_available, dim):
+    """Runs of ten steps captured as one graph (each step with its own rebuild
+    branch) against the same steps one graph each: bitwise the same state,
+    rebuilds and pair counts."""
+    from sph2d_gb300 import Solver, cases
+
+    case = _dam(nx=60, ny=30) if dim == 2 else cases.dam_break_3d(dx=0.02)
+    p = case.params()
+    out = []
+    for chunks in ((40,), (1,) * 40, (7, 13, 20)):
+        with Solver(p, "mixed") as s:
+            s.upload(case.r, case.v, case.rho, case.itype)
+            t = 0.0
+            for n in chunks:
+                t = s.step(n, t)
+            out.append((s.download(), s.neighbour_rebuilds(), s.pair_count(), t))
+    if dim == 2:
+        assert out[0][1] >= 2  # rebuilds fall inside the runs
+    for other in out[1:]:
+        assert other[1] == out[0][1] and other[2] == out[0][2] and other[3] == out[0][3]
+        for k in ("r", "v", "rho", "p"):
+            assert np.array_equal(out[0][0][k], other[0][k]), k
+
+
 def test_neighbour_reuse_across_uploads(gpu_available):
     """An upload keeps the candidate lists when every particle is within half
     the skin of the last build and the build left no particle out; one that
