@@ -726,16 +726,21 @@ def continuity_rate_error(steps: int = 1) -> dict:
     return {k: _rel(a[k], b[k]) for k in ("r", "v", "rho", "p", "a", "drho")}
 
 
-def reference_timing(case, p, warmup: int, steps: int) -> dict:
-    """The reference's CPU implementation of the step on all host cores, over
-    `warmup` untimed and `steps` timed steps from the seeded start: the
+REF_PHASES = ("predict", "grid_find", "density", "accel", "whole")
+
+
+def reference_timing(case, p, warmup: int, steps: int, threads: int = 0) -> dict:
+    """The reference's CPU implementation of the step on `threads` host threads
+    (0: all cores), over `warmup` untimed and `steps` timed steps from the
+    seeded start: the
     reference's own RRSPH_OMP compute core (oracle/_ref/rrsph_ref, built from
     its sources) where it was built, else the C restatement of it (oracle/).
     Time = the sum of the timed steps' wall times (no I/O)."""
     from oracle import binding as O
 
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     total = warmup + steps
+    phases = None
     if O.ref_available():
         out = O.ref_run(p, f"run:{total}", case.r, case.v, case.rho, case.itype, threads=threads, timeout=3600)
         step_ms = out["step_ms"]
@@ -743,6 +748,9 @@ def reference_timing(case, p, warmup: int, steps: int) -> dict:
         cores = int(out["timing"]["threads"])
         kind = "reference"
         what = "the reference's RRSPH_OMP compute core built from its sources (oracle/_ref/rrsph_ref)"
+        if "phase_ms" in out:
+            mean = out["phase_ms"][warmup:total].mean(axis=0)
+            phases = dict(zip(REF_PHASES, (float(x) for x in mean)))
     else:
         O.set_threads(threads)
         res = O.run(p, case.r, case.v, case.rho, case.itype, nsteps=warmup) if warmup else None
@@ -760,17 +768,23 @@ def reference_timing(case, p, warmup: int, steps: int) -> dict:
     t_ms = float(np.sum(step_ms[warmup:total]))
     timed_pairs = int(np.sum(pairs[warmup:total]))
     return {"kind": kind, "cores": cores, "ms_per_step": t_ms / steps, "value": timed_pairs / (t_ms / 1e3),
-            "pairs_first": int(pairs[0]), "pairs_timed": timed_pairs,
+            "pairs_first": int(pairs[0]), "pairs_timed": timed_pairs, "phases_ms_per_step": phases,
             "sample": f"steps {warmup + 1}-{total} of the {case.ntotal}-particle flume from the seeded start on "
                       f"{cores} threads: {what}; directed pairs of those steps / the sum of their wall times"}
 
 
-def cpu_baseline(case, p, steps: int) -> dict:
+def cpu_baseline(case, p, steps: int, one_thread_steps: int = 2) -> dict:
     """The reference's CPU step beside the GPU arm: a bounded sample of the
-    same workload (its first `steps` steps after one warm-up step)."""
+    same workload (its first `steps` steps after one warm-up step) on all host
+    cores, with its per-phase times, and a shorter sample on one thread."""
     r = reference_timing(case, p, 1, steps)
-    return {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": r["kind"], "sample": r["sample"],
-            "ms_per_step": r["ms_per_step"]}
+    out = {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": r["kind"], "sample": r["sample"],
+           "ms_per_step": r["ms_per_step"], "phases_ms_per_step": r["phases_ms_per_step"]}
+    if one_thread_steps > 0 and r["kind"] == "reference":
+        r1 = reference_timing(case, p, 1, one_thread_steps, threads=1)
+        out["one_thread"] = {"value": r1["value"], "ms_per_step": r1["ms_per_step"],
+                             "phases_ms_per_step": r1["phases_ms_per_step"], "sample": r1["sample"]}
+    return out
 
 
 def run_reference(args, rank: int, world: int) -> dict | None:
@@ -798,7 +812,8 @@ def run_reference(args, rank: int, world: int) -> dict | None:
         "config": workload_config(case, r["pairs_first"], args.warmup, args.steps),
         "method": {"precision": "f64 (the reference's rr_float)", "neighbour_search": "grid + stencil every step",
                    "threads": r["cores"]},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": r["cores"], "kind": r["kind"], "sample": r["sample"]},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": r["cores"], "kind": r["kind"], "sample": r["sample"],
+                         "phases_ms_per_step": r["phases_ms_per_step"]},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 

@@ -305,6 +305,8 @@ def ref_run(p, mode: str, r, v, rho, itype, pres=None, threads: int = 0, timeout
         for key in ("a", "av", "r_out", "v_out", "a_out"):
             if key in out:
                 out[key] = out[key].reshape(n, dim)
+        if "phase_ms" in out:  # per step: predict, grid_find, density, accel, whole
+            out["phase_ms"] = out["phase_ms"].reshape(-1, 5)
         if gauges is not None and "gauges" in out:
             out["gauges"] = out["gauges"].reshape(-1, len(gauges[3]))
         return out

@@ -13,7 +13,8 @@
 //   accel       update_acceleration                   (RRSPH_OMP/src/UpdateAcceleration.cpp:33-125)
 //   run:N       N iterations of the loop body of TimeIntegration.cpp:60-100 with the
 //               piston call enabled (dynamic_boundaries, WaveMaker.cpp:34-82),
-//               reporting wall time per phase and per step (step_ms.f64) and the
+//               reporting wall time per phase and per step (step_ms.f64; phase_ms.f64:
+//               per step predict, grid, density, accel, whole) and the
 //               directed pairs of every step's find_neighbours (pairs.u64, counted
 //               outside the timed phases); when
 //               case_dir holds gauges.txt ("every search_n type_filter" then the gauge
@@ -357,10 +358,12 @@ int main(int argc, char** argv) {
             };
             std::vector<uint64_t> pairs(nsteps);
             std::vector<double> step_ms(nsteps);
+            std::vector<double> phase_ms(5 * nsteps);  // per step: predict, grid, density, accel, whole
             if (gs.every) sample();
             auto t_all = std::chrono::steady_clock::now();
             for (unsigned long step = 0; step < nsteps; step++) {
                 const double phases_before = t_predict + t_grid + t_density + t_accel + t_whole;
+                const double before[5] = {t_predict, t_grid, t_density, t_accel, t_whole};
                 auto t0 = std::chrono::steady_clock::now();
                 predict_half_step(s.itype, s.rho, drho, s.v, a, rho_predict, v_predict);
                 t_predict += ms_since(t0);
@@ -394,6 +397,8 @@ int main(int argc, char** argv) {
                 whole_step(step, drho, a, av, s.itype, s.rho, s.v, s.r);
                 t_whole += ms_since(t0);
                 step_ms[step] = t_predict + t_grid + t_density + t_accel + t_whole - phases_before;
+                const double after[5] = {t_predict, t_grid, t_density, t_accel, t_whole};
+                for (int q = 0; q < 5; q++) phase_ms[5 * step + q] = after[q] - before[q];
                 time += params.dt;
                 if (gs.every && (step + 1) % gs.every == 0) {
                     t0 = std::chrono::steady_clock::now();
@@ -404,6 +409,7 @@ int main(int argc, char** argv) {
             const double total = ms_since(t_all) - t_aside;
             write_array("pairs.u64", pairs.data(), pairs.size());
             write_array("step_ms.f64", step_ms.data(), step_ms.size());
+            write_array("phase_ms.f64", phase_ms.data(), phase_ms.size());
             if (gs.every) write_array("gauges.f64", gauges.data(), gauges.size());
             auto fr = flat(s.r), fv = flat(s.v), fa = flat(a);
             write_array("r_out.f64", fr.data(), fr.size());
