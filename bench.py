@@ -357,7 +357,9 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         e2e_time[0] = tt.value
         capi.check(L.rrsph_download(sm.handle, dp(host["r"]), 2, dp(host["v"]), dp(host["rho"]), dp(host["p"]),
                                     ip(host["itype"])))
-        return sm.pair_count()[0]
+        pairs = C.c_uint64()  # the step's pairs, as rrsph_step read them back (no device access)
+        capi.check(L.rrsph_last_report(sm.handle, None, None, C.byref(pairs), None))
+        return pairs.value
 
     # 200 steps whatever K is (~85 ms): a stall of the host (the GPU machine's
     # cores are shared with other work) weighs little in the mean

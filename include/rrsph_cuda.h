@@ -269,6 +269,12 @@ int rrsph_download_rates(rrsph_solver* s, double* a, uint32_t stride, double* dr
 /* Directed neighbour pairs (the entries find_neighbours would list) of the
  * last completed step, and summed over the steps since rrsph_upload. */
 int rrsph_pair_count(rrsph_solver* s, uint64_t* last_step, uint64_t* total);
+/* What the last rrsph_step / rrsph_sync read back, without touching the
+ * device: the time after its last step, the device flags, and the pairs of
+ * rrsph_pair_count as of that call (any pointer may be NULL). All zero before
+ * the first rrsph_step / rrsph_sync. */
+int rrsph_last_report(rrsph_solver* s, double* time, uint32_t* flags, uint64_t* pairs_last,
+                      uint64_t* pairs_total);
 /* Current time step (changes under DT_CORRECTION_DYNAMIC with dt_dynamic_reduce). */
 int rrsph_get_dt(rrsph_solver* s, double* dt);
 

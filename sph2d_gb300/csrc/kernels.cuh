@@ -155,6 +155,8 @@ void launch_pack(const DevParams& P, State S, double* r, double* v, uint32_t str
 struct HostReport {
     double time;
     uint32_t flags;
+    unsigned long long pairs_last;   // directed pairs of the last completed step (0: none since upload)
+    unsigned long long pairs_total;  // summed over the steps since upload
 };
 void launch_set_time(StepScalars* scal, double time, uint32_t* flags, cudaStream_t st);
 // rrsph_diagnostics: blocks partial sums of kDiagQuantities doubles into part
@@ -162,7 +164,9 @@ void launch_set_time(StepScalars* scal, double time, uint32_t* flags, cudaStream
 constexpr int kDiagQuantities = 10;
 template <int DIM>
 void launch_diagnostics(const DevParams& P, const State& S, double* part, int blocks, double* out, cudaStream_t st);
-void launch_report(const StepScalars* scal, const uint32_t* flags, HostReport* out, cudaStream_t st);
+// scal: the next step's scalars; last: the completed step's (null: none since upload).
+void launch_report(const StepScalars* scal, const StepScalars* last, const uint32_t* flags, HostReport* out,
+                   cudaStream_t st);
 // Upload / download through device-addressable host arrays (pinned memory):
 // one kernel reading (writing) the caller's arrays over the host link. The
 // upload also runs the first step's predict + key pass (launch_keys).

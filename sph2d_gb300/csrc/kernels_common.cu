@@ -341,10 +341,12 @@ __global__ void k_set_time(StepScalars* __restrict__ scal, double time, uint32_t
     scal->time = time;
     if (flags) *flags = 0u;
 }
-__global__ void k_report(const StepScalars* __restrict__ scal, const uint32_t* __restrict__ flags,
-                         HostReport* __restrict__ out) {
+__global__ void k_report(const StepScalars* __restrict__ scal, const StepScalars* __restrict__ last,
+                         const uint32_t* __restrict__ flags, HostReport* __restrict__ out) {
     out->time = scal->time;
     out->flags = *flags;
+    out->pairs_last = last ? last->pairs : 0ull;
+    out->pairs_total = scal->pairs_total;
 }
 
 // rrsph_download into host arrays the device can address: one pass writing
@@ -380,8 +382,9 @@ void launch_diagnostics(const DevParams& P, const State& S, double* part, int bl
 void launch_set_time(StepScalars* scal, double time, uint32_t* flags, cudaStream_t st) {
     k_set_time<<<1, 1, 0, st>>>(scal, time, flags);
 }
-void launch_report(const StepScalars* scal, const uint32_t* flags, HostReport* out, cudaStream_t st) {
-    k_report<<<1, 1, 0, st>>>(scal, flags, out);
+void launch_report(const StepScalars* scal, const StepScalars* last, const uint32_t* flags, HostReport* out,
+                   cudaStream_t st) {
+    k_report<<<1, 1, 0, st>>>(scal, last, flags, out);
 }
 
 template <int DIM>

@@ -576,6 +576,7 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
         cudaHostAlloc(&s->h_report, sizeof(rrsph::HostReport), cudaHostAllocMapped) != cudaSuccess ||
         cudaHostGetDevicePointer((void**)&s->d_report, s->h_report, 0) != cudaSuccess)
         return fail(set_error(RRSPH_ERR_OUT_OF_MEMORY, "rrsph_create: pinned host allocation failed"));
+    std::memset(s->h_report, 0, sizeof(rrsph::HostReport));
     // empty cell table, zeroed state
     if (cudaMemsetAsync(G.cell_start, 0xFF, (size_t)s->P.max_cells * sizeof(uint32_t), s->stream) != cudaSuccess ||
         cudaMemsetAsync(S.key_of, 0xFF, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
@@ -867,7 +868,7 @@ extern "C" int rrsph_sync(rrsph_solver* s, double* time_out) {
     if (rc) return rc;
     cudaStream_t st = s->stream;
     const int parn = (int)(s->step_index & 1);
-    rrsph::launch_report(&s->scal[parn], s->flags, s->d_report, st);
+    rrsph::launch_report(&s->scal[parn], s->step_index ? &s->scal[parn ^ 1] : nullptr, s->flags, s->d_report, st);
     s->launches++;
     RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
     RRSPH_CUDA_TRY(cudaGetLastError());
@@ -884,6 +885,18 @@ extern "C" int rrsph_step(rrsph_solver* s, uint64_t nsteps, double* time_io) {
     s->launches++;
     if ((rc = enqueue_steps(s, nsteps)) != 0) return rc;
     return rrsph_sync(s, time_io);
+}
+
+extern "C" int rrsph_last_report(rrsph_solver* s, double* time, uint32_t* flags, uint64_t* pairs_last,
+                                 uint64_t* pairs_total) {
+    int rc = check_handle(s, "rrsph_last_report");
+    if (rc) return rc;
+    const rrsph::HostReport r = *s->h_report;  // written by the last rrsph_sync's report kernel
+    if (time) *time = r.time;
+    if (flags) *flags = r.flags;
+    if (pairs_last) *pairs_last = r.pairs_last;
+    if (pairs_total) *pairs_total = r.pairs_total;
+    return RRSPH_OK;
 }
 
 extern "C" int rrsph_status(rrsph_solver* s, uint32_t* flags, int clear) {

@@ -193,6 +193,13 @@ class Solver:
         check(lib().rrsph_pair_count(self._h, C.byref(a), C.byref(b)))
         return int(a.value), int(b.value)
 
+    def last_report(self) -> dict:
+        """What the last step()/sync() read back (no device access): time,
+        device flags, and the pair counts of pair_count() as of that call."""
+        t, f, a, b = C.c_double(), C.c_uint32(), C.c_uint64(), C.c_uint64()
+        check(lib().rrsph_last_report(self._h, C.byref(t), C.byref(f), C.byref(a), C.byref(b)))
+        return {"time": t.value, "flags": int(f.value), "pairs_last": int(a.value), "pairs_total": int(b.value)}
+
     def dt(self) -> float:
         d = C.c_double()
         check(lib().rrsph_get_dt(self._h, C.byref(d)))

@@ -529,6 +529,29 @@ def test_graph_replay_equals_direct_launches(gpu_available):
         assert np.array_equal(out[0][k], out[1][k]), k
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_last_report_is_what_the_step_read_back(gpu_available, precision):
+    """rrsph_last_report returns, without touching the device, the time, flags
+    and pair counts of the last rrsph_step / rrsph_sync."""
+    from sph2d_gb300 import Solver
+
+    case = _dam(nx=40, ny=20)
+    p = case.params()
+    with Solver(p, precision) as s:
+        assert s.last_report() == {"time": 0.0, "flags": 0, "pairs_last": 0, "pairs_total": 0}
+        s.upload(case.r, case.v, case.rho, case.itype)
+        t = s.step(3, 0.0)
+        rep = s.last_report()
+        assert rep["time"] == t and rep["flags"] == 0
+        assert (rep["pairs_last"], rep["pairs_total"]) == s.pair_count() and rep["pairs_last"] > 0
+        s.step_async(12)  # a 10-step graph and two single steps
+        t2 = s.sync()
+        rep2 = s.last_report()
+        assert rep2["time"] == t2 > t
+        assert (rep2["pairs_last"], rep2["pairs_total"]) == s.pair_count()
+        assert rep2["pairs_total"] > rep["pairs_total"]
+
+
 def test_stepping_in_chunks_equals_one_call(gpu_available):
     from sph2d_gb300 import Solver
 
