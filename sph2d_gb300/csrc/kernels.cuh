@@ -50,6 +50,7 @@ struct Sorted {
     double *rho;                      // density the forces use
     double *rhod;                     // density of density_con
     double* p;
+    double* pr2;                      // p / (rho * rho) with the density the forces use (the density pass writes it)
     int32_t* itype;
     // FP32-mixed gathers
     float4* P4;    // cell-relative position (x, y, z) + itype bits
@@ -62,10 +63,12 @@ struct Sorted {
     float4* P4n;
     float4* V4n;
     float4* VD4n;
-    // 2D mixed step: neighbour masks written by the density pass for the force
-    // pass, SoA [10][n]: word c < 9 = bit b set if particle cell_start + b of
-    // stencil cell c is a neighbour; word 9 = stencil cells with more than 32
-    // particles (searched again by the force pass). Null where unused.
+    // Neighbour masks written by the density pass for the force pass (the FP64
+    // step, 2D and 3D; the 2D mixed step without reuse), SoA [NC + 1][n] with
+    // NC = 3^dim stencil cells: word c < NC = bit b set if particle
+    // cell_start + b of stencil cell c is a neighbour; word NC = stencil cells
+    // with more than 32 particles (searched again by the force pass). Null
+    // where unused.
     uint32_t* nbmask;
     // mixed step with neighbour reuse: up to kVerletCap2 (2D) / kVerletCap3 (3D)
     // candidates per particle, sorted index | cell code << 27 (3D: << 25) with
@@ -100,9 +103,11 @@ void launch_reorder(const DevParams& P, const State& S, const Sorted& G, GatherS
 template <int DIM>
 void launch_density_fp64(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
                          cudaStream_t st, int threads);
+// use_masks: the pairs are those the density pass on this grid recorded in
+// G.nbmask (the same pairs in the same order as the search).
 template <int DIM>
 void launch_forces_fp64(const DevParams& P, const State& S, const Sorted& G, uint32_t terms, StepScalars* scal,
-                        uint32_t* flags, int write_mu, cudaStream_t st, int threads);
+                        uint32_t* flags, int write_mu, cudaStream_t st, int threads, int use_masks = 0);
 template <int DIM>
 void launch_density_mixed(const DevParams& P, const State& S, const Sorted& G, StepScalars* scal, uint32_t* flags,
                           cudaStream_t st, int threads);

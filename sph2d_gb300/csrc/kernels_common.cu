@@ -48,11 +48,18 @@ __global__ void k_reorder(DevParams P, State S, Sorted G, GatherSrc F) {
         G.itype[k] = t;
     }
     if (R == 0) {
+        if (G.P4) {  // the cell-relative float offsets of the FP64 density pass's first test
+            const float4 o = DIM == 3 ? S.coff4[id] : make_float4(S.coff2[id].x, S.coff2[id].y, 0.0f, 0.0f);
+            G.P4[k] = make_float4(o.x, o.y, o.z, __int_as_float(t));
+        }
         G.vx[k] = F.vx[id];
         G.vy[k] = F.vy[id];
         if (DIM == 3) G.vz[k] = F.vz[id];
         G.rho[k] = F.rho[id];
-        if (F.p) G.p[k] = F.p[id];
+        if (F.p) {  // a given pressure (rrsph_forces): p / rho^2 as the density pass writes it
+            G.p[k] = F.p[id];
+            G.pr2[k] = F.p[id] / (F.rho[id] * F.rho[id]);
+        }
         if (P.density_treatment != 0) {
             G.vdx[k] = S.vx[id];
             G.vdy[k] = S.vy[id];

@@ -48,21 +48,38 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density(DevParams P, Stat
         if (G.itype[k] != P.type_non_existent) {
             const Stencil<DIM> st(P, G.key[k]);
             constexpr int NC = DIM == 3 ? 27 : 9;
+            // the pairs found, per stencil cell, for the force pass (stored as the
+            // warp goes through the cells together: coalesced)
+            uint32_t* const masks = G.nbmask ? G.nbmask + k : nullptr;
+            uint32_t over = 0;
+            // the float test first: a particle whose float distance from the
+            // cell-relative offsets is beyond the cutoff's upper guard band is
+            // beyond the cutoff in double too; the others take the reference's test
+            const float4 pj4 = G.P4 ? G.P4[k] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            const float cellf = P.mf.cell, cut2_hi = G.P4 ? P.mf.cut2_hi : INFINITY;
 #pragma unroll 1
             for (int c = 0; c < NC; c++) {
+                uint32_t bits = 0;
                 uint32_t cell;
                 int sx, sy, sz;
-                if (!st.cell(c, cell, sx, sy, sz)) continue;
-                const uint32_t s = G.cell_start[cell];
-                if (s == kEmpty) continue;
-                const uint32_t e = G.cell_end[cell];
+                const uint32_t s = st.cell(c, cell, sx, sy, sz) ? G.cell_start[cell] : kEmpty;
+                const uint32_t e = s != kEmpty ? G.cell_end[cell] : s;
+                if (e - s > 32) over |= 1u << c;
+                const float shx = (float)sx * cellf - pj4.x, shy = (float)sy * cellf - pj4.y;
+                const float shz = DIM == 3 ? (float)sz * cellf - pj4.z : 0.0f;
                 for (uint32_t i = s; i < e; i++) {
                     if (i == k || G.itype[i] == P.type_non_existent) continue;
+                    if (G.P4) {
+                        const float4 pi4 = G.P4[i];
+                        const float fx = pi4.x + shx, fy = pi4.y + shy, fz = DIM == 3 ? pi4.z + shz : 0.0f;
+                        if (!(fx * fx + fy * fy + fz * fz < cut2_hi)) continue;
+                    }
                     const double dx = __dsub_rn(G.rx[i], xj), dy = __dsub_rn(G.ry[i], yj);
                     const double dz = DIM == 3 ? __dsub_rn(G.rz[i], zj) : 0.0;
                     const double d2 = exact_dist2<DIM>(dx, dy, dz);
                     if (!(d2 < P.cut2)) continue;
                     cnt++;
+                    if (i - s < 32) bits |= 1u << (i - s);
                     const double dist = sqrt(d2);
                     const double q = dist * P.inv_h;
                     if (!cont) {
@@ -85,18 +102,23 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density(DevParams P, Stat
                         }
                     }
                 }
+                if (masks) masks[(size_t)c * P.n] = bits;
             }
+            if (masks) masks[(size_t)NC * P.n] = over;
         }
         if (cnt > P.max_nb - 1) atomicOr(flags, RRSPH_FLAG_NEIGHBOUR_OVERFLOW);
         if (!cont) {
             const double pj = eos_p(P, acc);
             G.rho[k] = acc;
             G.p[k] = pj;
+            G.pr2[k] = pj / (acc * acc);
             S.rho[id] = acc;
             S.p[id] = pj;
         } else {
             const double pj = eos_p(P, rhoj);
+            const double rf = G.rho[k];  // the density the forces use (rho_predict)
             G.p[k] = pj;
+            G.pr2[k] = pj / (rf * rf);
             S.p[id] = pj;
             S.drho[id] = acc;
         }
@@ -111,7 +133,8 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density(DevParams P, Stat
 template <int DIM>
 __global__ void __launch_bounds__(kMaxGatherThreads) k_forces(DevParams P, State S, Sorted G, uint32_t terms,
                                                            StepScalars* __restrict__ scal,
-                                                           uint32_t* __restrict__ flags, int write_mu) {
+                                                           uint32_t* __restrict__ flags, int write_mu,
+                                                           int use_masks) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = k < P.n;
     double amag = 0, arvmu = 0;
@@ -128,9 +151,72 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_forces(DevParams P, State
         const bool visc = (terms & RRSPH_TERM_ART_VISC) && P.art_visc;
         const bool avel = (terms & RRSPH_TERM_AVERAGE_VELOCITY) && P.avg_vel;
         const double pj_r2 = pj / (rhoj * rhoj);
+        // the viscosity's kernel gradient is the pressure term's when both use one kernel
+        const bool same_skf = P.av_skf == P.intf_skf;
+        // the terms of one neighbour i (separation dx = r_i - r_j, d2 = |dx|^2)
+        auto pair = [&](uint32_t i, int32_t ti, double dx, double dy, double dz, double d2) {
+            const double dist = sqrt(d2);
+            const double q = dist * P.inv_h;
+            if (ext && ti < 0 && dist < P.lj_rr0) {
+                const double rn = P.lj_rr0 / dist;
+                const double rn2 = rn * rn, rn4 = rn2 * rn2, rn8 = rn4 * rn4;
+                const double fl = P.lj_D * (rn8 * rn4 - rn4) / d2;
+                ax -= dx * fl;
+                ay -= dy * fl;
+                if (DIM == 3) az -= dz * fl;
+            }
+            const double rhoi = G.rho[i];
+            double sc_intf = 0.0;
+            if (intf) {
+                const double pi = G.p[i];
+                const double sc = kernel_dwdr_scale(P.intf_skf, P.kf[P.intf_skf], q, dist, P.inv_h);
+                sc_intf = sc;
+                // p_i / rho_i^2: the density pass computed it per particle from the same values
+                double pf = P.intf_form == 1 ? (pj + pi) / (rhoj * rhoi) : (G.pr2[i] + pj_r2);
+                if (P.art_pressure && (pi < 0 || pj < 0)) {
+                    const double w = kernel_w(P.ap_skf, P.kf[P.ap_skf], q);
+                    const double api = pi < 0 ? (-P.ap_coef * pi / (rhoi * rhoi)) : 0.0;
+                    const double apj = pj < 0 ? (-P.ap_coef * pj / (rhoj * rhoj)) : 0.0;
+                    pf += (api + apj) * pow(w / P.ap_wdelta, P.ap_index);
+                }
+                const double m = sc * pf * P.mass;
+                ax += dx * m;
+                ay += dy * m;
+                if (DIM == 3) az += dz * m;
+            }
+            if (visc || avel) {
+                const double vxi = G.vx[i], vyi = G.vy[i], vzi = DIM == 3 ? G.vz[i] : 0.0;
+                if (visc) {
+                    // dv = v_j - v_i, dr = r_j - r_i = -diff
+                    double vr = -((vxj - vxi) * dx + (vyj - vyi) * dy);
+                    if (DIM == 3) vr -= (vzj - vzi) * dz;
+                    if (vr < 0) {
+                        const double mu = P.h * vr / (d2 + P.etq_h2);
+                        arvmu = fmax(arvmu, fabs(mu));
+                        const double rho_ij = 0.5 * (rhoi + rhoj);
+                        const double piv = (P.av_beta * mu - P.av_alpha * P.c_av) * mu / rho_ij;
+                        const double sc = intf && same_skf ? sc_intf
+                                                           : kernel_dwdr_scale(P.av_skf, P.kf[P.av_skf], q, dist, P.inv_h);
+                        const double m = sc * piv * P.mass;
+                        ax += dx * m;
+                        ay += dy * m;
+                        if (DIM == 3) az += dz * m;
+                    }
+                }
+                if (avel && ti > 0) {
+                    const double w = kernel_w(P.avel_skf, P.kf[P.avel_skf], q);
+                    const double m = P.mass / (rhoi + rhoj) * w * 2 * P.avg_vel_coef;
+                    avx += (vxi - vxj) * m;
+                    avy += (vyi - vyj) * m;
+                    if (DIM == 3) avz += (vzi - vzj) * m;
+                }
+            }
+        };
         if (tj != P.type_non_existent) {
             const Stencil<DIM> st(P, G.key[k]);
             constexpr int NC = DIM == 3 ? 27 : 9;
+            const uint32_t* const masks = use_masks ? G.nbmask + k : nullptr;
+            const uint32_t over = masks ? masks[(size_t)NC * P.n] : 0xFFFFFFFFu;
 #pragma unroll 1
             for (int c = 0; c < NC; c++) {
                 uint32_t cell;
@@ -138,6 +224,16 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_forces(DevParams P, State
                 if (!st.cell(c, cell, sx, sy, sz)) continue;
                 const uint32_t s = G.cell_start[cell];
                 if (s == kEmpty) continue;
+                if (!((over >> c) & 1u)) {
+                    // the neighbours the density pass found in this cell, ascending
+                    for (uint32_t bits = masks[(size_t)c * P.n]; bits; bits &= bits - 1) {
+                        const uint32_t i = s + (uint32_t)(__ffs(bits) - 1);
+                        const double dx = __dsub_rn(G.rx[i], xj), dy = __dsub_rn(G.ry[i], yj);
+                        const double dz = DIM == 3 ? __dsub_rn(G.rz[i], zj) : 0.0;
+                        pair(i, G.itype[i], dx, dy, dz, exact_dist2<DIM>(dx, dy, dz));
+                    }
+                    continue;
+                }
                 const uint32_t e = G.cell_end[cell];
                 for (uint32_t i = s; i < e; i++) {
                     if (i == k) continue;
@@ -147,58 +243,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_forces(DevParams P, State
                     const double dz = DIM == 3 ? __dsub_rn(G.rz[i], zj) : 0.0;
                     const double d2 = exact_dist2<DIM>(dx, dy, dz);
                     if (!(d2 < P.cut2)) continue;
-                    const double dist = sqrt(d2);
-                    const double q = dist * P.inv_h;
-                    if (ext && ti < 0 && dist < P.lj_rr0) {
-                        const double rn = P.lj_rr0 / dist;
-                        const double rn2 = rn * rn, rn4 = rn2 * rn2, rn8 = rn4 * rn4;
-                        const double fl = P.lj_D * (rn8 * rn4 - rn4) / d2;
-                        ax -= dx * fl;
-                        ay -= dy * fl;
-                        if (DIM == 3) az -= dz * fl;
-                    }
-                    const double rhoi = G.rho[i];
-                    if (intf) {
-                        const double pi = G.p[i];
-                        const double sc = kernel_dwdr_scale(P.intf_skf, P.kf[P.intf_skf], q, dist, P.inv_h);
-                        double pf = P.intf_form == 1 ? (pj + pi) / (rhoj * rhoi) : (pi / (rhoi * rhoi) + pj_r2);
-                        if (P.art_pressure && (pi < 0 || pj < 0)) {
-                            const double w = kernel_w(P.ap_skf, P.kf[P.ap_skf], q);
-                            const double api = pi < 0 ? (-P.ap_coef * pi / (rhoi * rhoi)) : 0.0;
-                            const double apj = pj < 0 ? (-P.ap_coef * pj / (rhoj * rhoj)) : 0.0;
-                            pf += (api + apj) * pow(w / P.ap_wdelta, P.ap_index);
-                        }
-                        const double m = sc * pf * P.mass;
-                        ax += dx * m;
-                        ay += dy * m;
-                        if (DIM == 3) az += dz * m;
-                    }
-                    if (visc || avel) {
-                        const double vxi = G.vx[i], vyi = G.vy[i], vzi = DIM == 3 ? G.vz[i] : 0.0;
-                        if (visc) {
-                            // dv = v_j - v_i, dr = r_j - r_i = -diff
-                            double vr = -((vxj - vxi) * dx + (vyj - vyi) * dy);
-                            if (DIM == 3) vr -= (vzj - vzi) * dz;
-                            if (vr < 0) {
-                                const double mu = P.h * vr / (d2 + P.etq_h2);
-                                arvmu = fmax(arvmu, fabs(mu));
-                                const double rho_ij = 0.5 * (rhoi + rhoj);
-                                const double piv = (P.av_beta * mu - P.av_alpha * P.c_av) * mu / rho_ij;
-                                const double sc = kernel_dwdr_scale(P.av_skf, P.kf[P.av_skf], q, dist, P.inv_h);
-                                const double m = sc * piv * P.mass;
-                                ax += dx * m;
-                                ay += dy * m;
-                                if (DIM == 3) az += dz * m;
-                            }
-                        }
-                        if (avel && ti > 0) {
-                            const double w = kernel_w(P.avel_skf, P.kf[P.avel_skf], q);
-                            const double m = P.mass / (rhoi + rhoj) * w * 2 * P.avg_vel_coef;
-                            avx += (vxi - vxj) * m;
-                            avy += (vyi - vyj) * m;
-                            if (DIM == 3) avz += (vzi - vzj) * m;
-                        }
-                    }
+                    pair(i, ti, dx, dy, dz, d2);
                 }
             }
         }
@@ -228,8 +273,9 @@ void launch_density_fp64(const DevParams& P, const State& S, const Sorted& G, St
 }
 template <int DIM>
 void launch_forces_fp64(const DevParams& P, const State& S, const Sorted& G, uint32_t terms, StepScalars* scal,
-                        uint32_t* flags, int write_mu, cudaStream_t st, int threads) {
-    k_forces<DIM><<<(P.n + threads - 1) / threads, threads, 0, st>>>(P, S, G, terms, scal, flags, write_mu);
+                        uint32_t* flags, int write_mu, cudaStream_t st, int threads, int use_masks) {
+    k_forces<DIM><<<(P.n + threads - 1) / threads, threads, 0, st>>>(P, S, G, terms, scal, flags, write_mu,
+                                                                    use_masks && G.nbmask ? 1 : 0);
 }
 
 template void launch_density_fp64<2>(const DevParams&, const State&, const Sorted&, StepScalars*, uint32_t*,
@@ -237,8 +283,8 @@ template void launch_density_fp64<2>(const DevParams&, const State&, const Sorte
 template void launch_density_fp64<3>(const DevParams&, const State&, const Sorted&, StepScalars*, uint32_t*,
                                      cudaStream_t, int);
 template void launch_forces_fp64<2>(const DevParams&, const State&, const Sorted&, uint32_t, StepScalars*, uint32_t*,
-                                    int, cudaStream_t, int);
+                                    int, cudaStream_t, int, int);
 template void launch_forces_fp64<3>(const DevParams&, const State&, const Sorted&, uint32_t, StepScalars*, uint32_t*,
-                                    int, cudaStream_t, int);
+                                    int, cudaStream_t, int, int);
 
 }  // namespace rrsph

@@ -233,7 +233,7 @@ void enqueue_forces(rrsph_solver* s, uint32_t terms, rrsph::StepScalars* scal, i
     const int th = s->gather_threads[1];
     if (s->precision == RRSPH_PRECISION_MIXED)
         rrsph::launch_forces_mixed<DIM>(s->P, s->S, s->G, terms, scal, s->flags, write_mu, use_masks, s->stream, th);
-    else rrsph::launch_forces_fp64<DIM>(s->P, s->S, s->G, terms, scal, s->flags, write_mu, s->stream, th);
+    else rrsph::launch_forces_fp64<DIM>(s->P, s->S, s->G, terms, scal, s->flags, write_mu, s->stream, th, use_masks);
     s->launches++;
 }
 
@@ -507,7 +507,12 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
     A(G.itype, n);
     if (!mixed) {
         A(G.vx, n); A(G.vy, n); if (d3) A(G.vz, n);
-        A(G.rho, n); A(G.p, n);
+        A(G.rho, n); A(G.p, n); A(G.pr2, n);
+        A(G.nbmask, (size_t)(d3 ? 28 : 10) * n);  // the density pass's pairs for the force pass
+        // cell-relative float offsets (key pass) and their cell-order copy: the
+        // density pass's float test rejects the stencil particles beyond the cutoff
+        if (d3) A(S.coff4, n); else A(S.coff2, n);
+        A(G.P4, n);
         if (cont) { A(G.vdx, n); A(G.vdy, n); if (d3) A(G.vdz, n); A(G.rhod, n); }
     } else {
         if (d3) { A(S.coff4, n); A(S.vpf4, n); } else { A(S.coff2, n); A(S.vpf2, n); }

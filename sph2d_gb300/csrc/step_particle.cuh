@@ -95,7 +95,7 @@ __device__ __forceinline__ void key_pass(const DevParams& P, const State& S, con
     S.key_of[i] = (uint32_t)key;
     G.keys_in[i] = (uint32_t)key;
     G.ids_in[i] = i;
-    if (M == 0) return;
+    if (M == 0 && !(DIM == 3 ? (void*)S.coff4 : (void*)S.coff2)) return;
     // offsets from the edge of the cell the key names: the Morton code keeps 16
     // bits per axis in 2D and 10 in 3D (GridUtils.h:50-64, 92-104). A cell
     // coordinate whose key lies in the grid fits in 32 bits, so the dropped bits
