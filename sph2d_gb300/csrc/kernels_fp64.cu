@@ -48,63 +48,111 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density(DevParams P, Stat
         if (G.itype[k] != P.type_non_existent) {
             const Stencil<DIM> st(P, G.key[k]);
             constexpr int NC = DIM == 3 ? 27 : 9;
-            // the pairs found, per stencil cell, for the force pass (stored as the
-            // warp goes through the cells together: coalesced)
-            uint32_t* const masks = G.nbmask ? G.nbmask + k : nullptr;
+            uint32_t* const masks = G.nbmask + k;  // [c * n]: this particle's bits of stencil cell c
+            const float4 pj4 = G.P4[k];
+            const float cellf = P.mf.cell, cut2_hi = P.mf.cut2_hi;
+            // 1. The float test on the cell-relative offsets: a particle beyond the
+            // cutoff's upper guard band is beyond the cutoff in double too; the
+            // others are candidates (bit b of cell c: particle cell_start + b). A cell
+            // of more than 32 particles is searched in place below. The warp goes
+            // through the cells together, so the mask stores are coalesced.
             uint32_t over = 0;
-            // the float test first: a particle whose float distance from the
-            // cell-relative offsets is beyond the cutoff's upper guard band is
-            // beyond the cutoff in double too; the others take the reference's test
-            const float4 pj4 = G.P4 ? G.P4[k] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            const float cellf = P.mf.cell, cut2_hi = G.P4 ? P.mf.cut2_hi : INFINITY;
 #pragma unroll 1
             for (int c = 0; c < NC; c++) {
-                uint32_t bits = 0;
+                uint32_t cand = 0;
                 uint32_t cell;
                 int sx, sy, sz;
                 const uint32_t s = st.cell(c, cell, sx, sy, sz) ? G.cell_start[cell] : kEmpty;
                 const uint32_t e = s != kEmpty ? G.cell_end[cell] : s;
-                if (e - s > 32) over |= 1u << c;
-                const float shx = (float)sx * cellf - pj4.x, shy = (float)sy * cellf - pj4.y;
-                const float shz = DIM == 3 ? (float)sz * cellf - pj4.z : 0.0f;
-                for (uint32_t i = s; i < e; i++) {
-                    if (i == k || G.itype[i] == P.type_non_existent) continue;
-                    if (G.P4) {
+                if (e - s > 32) {
+                    over |= 1u << c;
+                } else {
+                    const float shx = (float)sx * cellf - pj4.x, shy = (float)sy * cellf - pj4.y;
+                    const float shz = DIM == 3 ? (float)sz * cellf - pj4.z : 0.0f;
+                    for (uint32_t i = s; i < e; i++) {
                         const float4 pi4 = G.P4[i];
                         const float fx = pi4.x + shx, fy = pi4.y + shy, fz = DIM == 3 ? pi4.z + shz : 0.0f;
-                        if (!(fx * fx + fy * fy + fz * fz < cut2_hi)) continue;
-                    }
-                    const double dx = __dsub_rn(G.rx[i], xj), dy = __dsub_rn(G.ry[i], yj);
-                    const double dz = DIM == 3 ? __dsub_rn(G.rz[i], zj) : 0.0;
-                    const double d2 = exact_dist2<DIM>(dx, dy, dz);
-                    if (!(d2 < P.cut2)) continue;
-                    cnt++;
-                    if (i - s < 32) bits |= 1u << (i - s);
-                    const double dist = sqrt(d2);
-                    const double q = dist * P.inv_h;
-                    if (!cont) {
-                        acc += P.mass * kernel_w(skf, f, q);
-                    } else {
-                        // diff = r_i - r_j; dwdr = diff * s
-                        const double sc = kernel_dwdr_scale(skf, f, q, dist, P.inv_h);
-                        const double gx = dx * sc, gy = dy * sc, gz = dz * sc;
-                        double vcc = (G.vdx[i] - vxj) * gx + (G.vdy[i] - vyj) * gy;
-                        if (DIM == 3) vcc += (G.vdz[i] - vzj) * gz;
-                        acc += P.mass * vcc;
-                        if (P.density_treatment == 2) {
-                            // r_ab = r_j - r_i = -diff
-                            double rd = -(dx * gx + dy * gy);
-                            if (DIM == 3) rd -= dz * gz;
-                            const double r_factor = rd / d2;
-                            const double rhoi = G.rhod[i];
-                            const double rho_factor = (rhoi - rhoj) / rhoi;
-                            acc += 2 * P.delta_sph_dhc * (rho_factor * r_factor) * P.mass;
-                        }
+                        const bool cnd = i != k && __float_as_int(pi4.w) != P.type_non_existent &&
+                                         fx * fx + fy * fy + fz * fz < cut2_hi;
+                        cand |= (cnd ? 1u : 0u) << (i - s);
                     }
                 }
-                if (masks) masks[(size_t)c * P.n] = bits;
+                masks[(size_t)c * P.n] = cand;
             }
-            if (masks) masks[(size_t)NC * P.n] = over;
+            masks[(size_t)NC * P.n] = over;
+            // 2. The candidates in the search's order (cells in stencil order, ids
+            // ascending) as one flat sequence, so the lanes of a warp run the double
+            // test and terms together (a warp's FP64 instruction costs the pipe the
+            // same time whatever lanes are active). A cell's neighbours replace its
+            // candidates in the masks the force pass reads.
+            int c = -1;
+            uint32_t bits = 0, base = 0, kept = 0;  // candidates left in a masked cell, and its neighbours
+            uint32_t next = 0, end = 0;             // or the range of a searched cell left
+            bool masked = false;
+            for (;;) {
+                if (bits == 0 && next == end) {
+                    if (masked) masks[(size_t)c * P.n] = kept;
+                    masked = false;
+                    for (c++; c < NC; c++) {
+                        uint32_t cell;
+                        int sx, sy, sz;
+                        if ((over >> c) & 1u) {  // a valid, non-empty cell
+                            st.cell(c, cell, sx, sy, sz);
+                            next = G.cell_start[cell];
+                            end = G.cell_end[cell];
+                            break;
+                        }
+                        bits = masks[(size_t)c * P.n];
+                        if (bits) {
+                            st.cell(c, cell, sx, sy, sz);
+                            base = G.cell_start[cell];
+                            kept = 0;
+                            masked = true;
+                            break;
+                        }
+                    }
+                    if (c >= NC) break;
+                }
+                uint32_t i, b = 0;
+                bool searched;
+                if (bits) {
+                    b = (uint32_t)(__ffs(bits) - 1);
+                    i = base + b;
+                    bits &= bits - 1;
+                    searched = false;
+                } else {
+                    i = next++;
+                    searched = true;
+                }
+                const double dx = __dsub_rn(G.rx[i], xj), dy = __dsub_rn(G.ry[i], yj);
+                const double dz = DIM == 3 ? __dsub_rn(G.rz[i], zj) : 0.0;
+                const double d2 = exact_dist2<DIM>(dx, dy, dz);
+                if (!(d2 < P.cut2)) continue;
+                if (searched && (i == k || G.itype[i] == P.type_non_existent)) continue;
+                cnt++;
+                kept |= (searched ? 0u : 1u) << b;
+                const double dist = sqrt(d2);
+                const double q = dist * P.inv_h;
+                if (!cont) {
+                    acc += P.mass * kernel_w(skf, f, q);
+                } else {
+                    // diff = r_i - r_j; dwdr = diff * s
+                    const double sc = kernel_dwdr_scale(skf, f, q, dist, P.inv_h);
+                    const double gx = dx * sc, gy = dy * sc, gz = dz * sc;
+                    double vcc = (G.vdx[i] - vxj) * gx + (G.vdy[i] - vyj) * gy;
+                    if (DIM == 3) vcc += (G.vdz[i] - vzj) * gz;
+                    acc += P.mass * vcc;
+                    if (P.density_treatment == 2) {
+                        // r_ab = r_j - r_i = -diff
+                        double rd = -(dx * gx + dy * gy);
+                        if (DIM == 3) rd -= dz * gz;
+                        const double r_factor = rd / d2;
+                        const double rhoi = G.rhod[i];
+                        const double rho_factor = (rhoi - rhoj) / rhoi;
+                        acc += 2 * P.delta_sph_dhc * (rho_factor * r_factor) * P.mass;
+                    }
+                }
+            }
         }
         if (cnt > P.max_nb - 1) atomicOr(flags, RRSPH_FLAG_NEIGHBOUR_OVERFLOW);
         if (!cont) {
@@ -217,34 +265,50 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_forces(DevParams P, State
             constexpr int NC = DIM == 3 ? 27 : 9;
             const uint32_t* const masks = use_masks ? G.nbmask + k : nullptr;
             const uint32_t over = masks ? masks[(size_t)NC * P.n] : 0xFFFFFFFFu;
-#pragma unroll 1
-            for (int c = 0; c < NC; c++) {
-                uint32_t cell;
-                int sx, sy, sz;
-                if (!st.cell(c, cell, sx, sy, sz)) continue;
-                const uint32_t s = G.cell_start[cell];
-                if (s == kEmpty) continue;
-                if (!((over >> c) & 1u)) {
-                    // the neighbours the density pass found in this cell, ascending
-                    for (uint32_t bits = masks[(size_t)c * P.n]; bits; bits &= bits - 1) {
-                        const uint32_t i = s + (uint32_t)(__ffs(bits) - 1);
-                        const double dx = __dsub_rn(G.rx[i], xj), dy = __dsub_rn(G.ry[i], yj);
-                        const double dz = DIM == 3 ? __dsub_rn(G.rz[i], zj) : 0.0;
-                        pair(i, G.itype[i], dx, dy, dz, exact_dist2<DIM>(dx, dy, dz));
+            // One flat sequence over the stencil cells: each iteration takes this
+            // particle's next candidate (the next neighbour the density pass recorded
+            // in a cell, or the next particle of a cell searched in place: more than
+            // 32 particles, or no masks), so the lanes of a warp run the double pair
+            // body together (a warp's FP64 instruction costs the pipe the same time
+            // whatever lanes are active). The order is the search's: cells in
+            // stencil order, ids ascending.
+            int c = -1;
+            uint32_t bits = 0, base = 0;  // the recorded neighbours of the current cell
+            uint32_t next = 0, end = 0;   // or the range left to search
+            for (;;) {
+                if (bits == 0 && next == end) {
+                    for (c++; c < NC; c++) {
+                        uint32_t cell;
+                        int sx, sy, sz;
+                        if (!st.cell(c, cell, sx, sy, sz)) continue;
+                        const uint32_t s = G.cell_start[cell];
+                        if (s == kEmpty) continue;
+                        if ((over >> c) & 1u) {
+                            next = s;
+                            end = G.cell_end[cell];
+                            break;
+                        }
+                        bits = masks[(size_t)c * P.n];
+                        base = s;
+                        if (bits) break;
                     }
-                    continue;
+                    if (c >= NC) break;
                 }
-                const uint32_t e = G.cell_end[cell];
-                for (uint32_t i = s; i < e; i++) {
-                    if (i == k) continue;
-                    const int32_t ti = G.itype[i];
-                    if (ti == P.type_non_existent) continue;
-                    const double dx = __dsub_rn(G.rx[i], xj), dy = __dsub_rn(G.ry[i], yj);
-                    const double dz = DIM == 3 ? __dsub_rn(G.rz[i], zj) : 0.0;
-                    const double d2 = exact_dist2<DIM>(dx, dy, dz);
-                    if (!(d2 < P.cut2)) continue;
-                    pair(i, ti, dx, dy, dz, d2);
+                uint32_t i;
+                bool known;
+                if (bits) {
+                    i = base + (uint32_t)(__ffs(bits) - 1);
+                    bits &= bits - 1;
+                    known = true;
+                } else {
+                    i = next++;
+                    known = false;
                 }
+                const int32_t ti = G.itype[i];
+                const double dx = __dsub_rn(G.rx[i], xj), dy = __dsub_rn(G.ry[i], yj);
+                const double dz = DIM == 3 ? __dsub_rn(G.rz[i], zj) : 0.0;
+                const double d2 = exact_dist2<DIM>(dx, dy, dz);
+                if (known || (i != k && ti != P.type_non_existent && d2 < P.cut2)) pair(i, ti, dx, dy, dz, d2);
             }
         }
         S.ax[id] = ax;
