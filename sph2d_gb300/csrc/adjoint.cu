@@ -121,8 +121,8 @@ __global__ void k_gauge_arg(uint32_t n, const double* __restrict__ rx, const dou
 // Cell-order copies of step n's forward quantities (the grid of r^n), and the
 // adjoint of whole_step and the piston: from the adjoints of S^{n+1} to those
 // before the step's updates, and λa of step n in cell order.
-__global__ void k_adj_reorder(DevParams P, Sorted G, SnapView sn, const double* __restrict__ rho_n, AdjBuf A,
-                              double dt, double v_dt, int piston) {
+__global__ void k_adj_reorder(DevParams P, Sorted G, SnapView sn, const double* __restrict__ rho_n,
+                              const float2* __restrict__ coff, AdjBuf A, double dt, double v_dt, int piston) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= P.n) return;
     const uint32_t key = G.key[k];
@@ -139,6 +139,8 @@ __global__ void k_adj_reorder(DevParams P, Sorted G, SnapView sn, const double* 
     G.rho[k] = rho;
     G.p[k] = p;
     G.itype[k] = t;
+    const float2 o = coff[id];  // the key pass's cell-relative offsets of r^n (the float first test)
+    G.P4[k] = make_float4(o.x, o.y, 0.0f, __int_as_float(t));
     A.pr2[k] = p / (rho * rho);
     double lrx = A.in_rx[id], lry = A.in_ry[id], lvx = A.in_vx[id], lvy = A.in_vy[id];
     double lax = A.in_ax[id], lay = A.in_ay[id];
@@ -179,76 +181,137 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_forces(DevParams P, Sorted 
         const double m = P.mass;
         const double ac = P.av_alpha * P.c_av;
         const bool form1 = P.intf_form == 1;
+        uint32_t* const masks = G.nbmask + k;  // [c * n]: this particle's bits of stencil cell c
         const Stencil<2> st(P, G.key[k]);
+        const float4 pj4 = G.P4[k];
+        // 1. Candidates by the float test on the cell-relative offsets (a particle
+        // beyond the cutoff's upper guard band is beyond it in double too); a cell
+        // of more than 32 particles is searched in place below.
+        uint32_t over = 0;
 #pragma unroll 1
         for (int c = 0; c < 9; c++) {
+            uint32_t cand = 0;
             uint32_t cell;
             int sx, sy, sz;
-            if (!st.cell(c, cell, sx, sy, sz)) continue;
-            const uint32_t s = G.cell_start[cell];
-            if (s == kEmpty) continue;
-            const uint32_t e = G.cell_end[cell];
-            for (uint32_t i = s; i < e; i++) {
-                if (i == k) continue;
-                const int32_t ti = G.itype[i];
-                if (ti == P.type_non_existent) continue;
-                const double ex = __dsub_rn(G.rx[i], xj), ey = __dsub_rn(G.ry[i], yj);
-                const double s2 = exact_dist2<2>(ex, ey, 0.0);
-                if (!(s2 < P.cut2)) continue;
-                const double inv_d = rsqrt(s2);
-                const double q = s2 * inv_d * P.inv_h;
-                double sc, sc1d;
-                cubic_sc(P, q, inv_d, sc, sc1d);
-                const double lx = laxj - A.la_x[i], ly = layj - A.la_y[i];
-                const double le = lx * ex + ly * ey;
-                const double rhoi = G.rho[i];
-                double PF, PFr, PFp;  // PF, dPF/drho_j, dPF/dp_j
-                if (form1) {
-                    const double inv = 1.0 / (rhoj * rhoi);
-                    PF = (pj + G.p[i]) * inv;
-                    PFr = -PF / rhoj;
-                    PFp = inv;
-                } else {
-                    PF = A.pr2[i] + pr2j;
-                    PFr = -2.0 * pr2j / rhoj;
-                    PFp = 1.0 / (rhoj * rhoj);
+            const uint32_t s = st.cell(c, cell, sx, sy, sz) ? G.cell_start[cell] : kEmpty;
+            const uint32_t e = s != kEmpty ? G.cell_end[cell] : s;
+            if (e - s > 32) {
+                over |= 1u << c;
+            } else {
+                const float shx = (float)sx * P.mf.cell - pj4.x, shy = (float)sy * P.mf.cell - pj4.y;
+                for (uint32_t i = s; i < e; i++) {
+                    const float4 pi4 = G.P4[i];
+                    const float fx = pi4.x + shx, fy = pi4.y + shy;
+                    const bool cnd = i != k && __float_as_int(pi4.w) != P.type_non_existent &&
+                                     fx * fx + fy * fy < P.mf.cut2_hi;
+                    cand |= (cnd ? 1u : 0u) << (i - s);
                 }
-                double Pi = 0, Pimu = 0, coefE, coefDv = 0, inv_rbar = 0;
-                const double dvx = vxj - G.vx[i], dvy = vyj - G.vy[i];
-                const double vr = -(dvx * ex + dvy * ey);
-                if (P.art_visc && vr < 0) {
-                    const double den = 1.0 / (s2 + P.etq_h2);
-                    const double mu = P.h * vr * den;
-                    inv_rbar = 2.0 / (rhoi + rhoj);
-                    Pi = (P.av_beta * mu - ac) * mu * inv_rbar;
-                    Pimu = (2.0 * P.av_beta * mu - ac) * inv_rbar;
-                    coefDv = -m * sc * Pimu * P.h * den;
-                    coefE = m * (sc1d * (PF + Pi) - 2.0 * sc * Pimu * P.h * vr * den * den);
-                } else {
-                    coefE = m * sc1d * PF;
-                }
-                const double S = m * sc * (PF + Pi);
-                // ∂ℓ/∂e = Λ S + (Λ·e) ∂S/∂e; r_j enters e with a minus sign
-                grx -= lx * S + le * (coefE * ex + coefDv * dvx);
-                gry -= ly * S + le * (coefE * ey + coefDv * dvy);
-                gvx += le * coefDv * ex;
-                gvy += le * coefDv * ey;
-                const double msc = m * sc * le;
-                grho += msc * (PFr - 0.5 * Pi * inv_rbar);
-                gp += msc * PFp;
-                if (P.repulsive && s2 * inv_d < P.lj_rr0) {
-                    const bool sj = tj > 0 && ti < 0, si = ti > 0 && tj < 0;
-                    if (sj || si) {
-                        const double Lx = sj ? laxj : -A.la_x[i], Ly = sj ? layj : -A.la_y[i];
-                        const double rn = P.lj_rr0 * inv_d;
-                        const double rn2 = rn * rn, rn4 = rn2 * rn2, rn12 = rn4 * rn4 * rn4;
-                        const double inv_s = inv_d * inv_d;
-                        const double fl = P.lj_D * (rn12 - rn4) * inv_s;
-                        const double fls = P.lj_D * (-7.0 * rn12 + 3.0 * rn4) * inv_s * inv_s;
-                        const double LE = Lx * ex + Ly * ey;
-                        grx += Lx * fl + 2.0 * LE * fls * ex;
-                        gry += Ly * fl + 2.0 * LE * fls * ey;
+            }
+            masks[(size_t)c * P.n] = cand;
+        }
+        masks[(size_t)9 * P.n] = over;
+        // 2. The candidates as one flat sequence (cells in stencil order, ids
+        // ascending): the forward step's double test, then the pair's adjoint
+        // terms, with the lanes of a warp together; a cell's neighbours replace
+        // its candidates in the masks (the density adjoint reads them).
+        int c = -1;
+        uint32_t bits = 0, base = 0, kept = 0;
+        uint32_t next = 0, end = 0;
+        bool masked = false;
+        for (;;) {
+            if (bits == 0 && next == end) {
+                if (masked) masks[(size_t)c * P.n] = kept;
+                masked = false;
+                for (c++; c < 9; c++) {
+                    uint32_t cell;
+                    int sx, sy, sz;
+                    if ((over >> c) & 1u) {
+                        st.cell(c, cell, sx, sy, sz);
+                        next = G.cell_start[cell];
+                        end = G.cell_end[cell];
+                        break;
                     }
+                    bits = masks[(size_t)c * P.n];
+                    if (bits) {
+                        st.cell(c, cell, sx, sy, sz);
+                        base = G.cell_start[cell];
+                        kept = 0;
+                        masked = true;
+                        break;
+                    }
+                }
+                if (c >= 9) break;
+            }
+            uint32_t i, b = 0;
+            bool searched;
+            if (bits) {
+                b = (uint32_t)(__ffs(bits) - 1);
+                i = base + b;
+                bits &= bits - 1;
+                searched = false;
+            } else {
+                i = next++;
+                searched = true;
+            }
+            const int32_t ti = G.itype[i];
+            const double ex = __dsub_rn(G.rx[i], xj), ey = __dsub_rn(G.ry[i], yj);
+            const double s2 = exact_dist2<2>(ex, ey, 0.0);
+            if (!(s2 < P.cut2)) continue;
+            if (searched && (i == k || ti == P.type_non_existent)) continue;
+            kept |= (searched ? 0u : 1u) << b;
+            const double inv_d = rsqrt(s2);
+            const double q = s2 * inv_d * P.inv_h;
+            double sc, sc1d;
+            cubic_sc(P, q, inv_d, sc, sc1d);
+            const double lx = laxj - A.la_x[i], ly = layj - A.la_y[i];
+            const double le = lx * ex + ly * ey;
+            const double rhoi = G.rho[i];
+            double PF, PFr, PFp;  // PF, dPF/drho_j, dPF/dp_j
+            if (form1) {
+                const double inv = 1.0 / (rhoj * rhoi);
+                PF = (pj + G.p[i]) * inv;
+                PFr = -PF / rhoj;
+                PFp = inv;
+            } else {
+                PF = A.pr2[i] + pr2j;
+                PFr = -2.0 * pr2j / rhoj;
+                PFp = 1.0 / (rhoj * rhoj);
+            }
+            double Pi = 0, Pimu = 0, coefE, coefDv = 0, inv_rbar = 0;
+            const double dvx = vxj - G.vx[i], dvy = vyj - G.vy[i];
+            const double vr = -(dvx * ex + dvy * ey);
+            if (P.art_visc && vr < 0) {
+                const double den = 1.0 / (s2 + P.etq_h2);
+                const double mu = P.h * vr * den;
+                inv_rbar = 2.0 / (rhoi + rhoj);
+                Pi = (P.av_beta * mu - ac) * mu * inv_rbar;
+                Pimu = (2.0 * P.av_beta * mu - ac) * inv_rbar;
+                coefDv = -m * sc * Pimu * P.h * den;
+                coefE = m * (sc1d * (PF + Pi) - 2.0 * sc * Pimu * P.h * vr * den * den);
+            } else {
+                coefE = m * sc1d * PF;
+            }
+            const double S = m * sc * (PF + Pi);
+            // ∂ℓ/∂e = Λ S + (Λ·e) ∂S/∂e; r_j enters e with a minus sign
+            grx -= lx * S + le * (coefE * ex + coefDv * dvx);
+            gry -= ly * S + le * (coefE * ey + coefDv * dvy);
+            gvx += le * coefDv * ex;
+            gvy += le * coefDv * ey;
+            const double msc = m * sc * le;
+            grho += msc * (PFr - 0.5 * Pi * inv_rbar);
+            gp += msc * PFp;
+            if (P.repulsive && s2 * inv_d < P.lj_rr0) {
+                const bool sj = tj > 0 && ti < 0, si = ti > 0 && tj < 0;
+                if (sj || si) {
+                    const double Lx = sj ? laxj : -A.la_x[i], Ly = sj ? layj : -A.la_y[i];
+                    const double rn = P.lj_rr0 * inv_d;
+                    const double rn2 = rn * rn, rn4 = rn2 * rn2, rn12 = rn4 * rn4 * rn4;
+                    const double inv_s = inv_d * inv_d;
+                    const double fl = P.lj_D * (rn12 - rn4) * inv_s;
+                    const double fls = P.lj_D * (-7.0 * rn12 + 3.0 * rn4) * inv_s * inv_s;
+                    const double LE = Lx * ex + Ly * ey;
+                    grx += Lx * fl + 2.0 * LE * fls * ex;
+                    gry += Ly * fl + 2.0 * LE * fls * ey;
                 }
             }
         }
@@ -272,26 +335,50 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_density(DevParams P, Sorted
     const double lj = A.lrho[k];
     double grx = 0, gry = 0;
     const Stencil<2> st(P, G.key[k]);
-#pragma unroll 1
-    for (int c = 0; c < 9; c++) {
-        uint32_t cell;
-        int sx, sy, sz;
-        if (!st.cell(c, cell, sx, sy, sz)) continue;
-        const uint32_t s = G.cell_start[cell];
-        if (s == kEmpty) continue;
-        const uint32_t e = G.cell_end[cell];
-        for (uint32_t i = s; i < e; i++) {
-            if (i == k || G.itype[i] == P.type_non_existent) continue;
-            const double ex = __dsub_rn(G.rx[i], xj), ey = __dsub_rn(G.ry[i], yj);
-            const double s2 = exact_dist2<2>(ex, ey, 0.0);
-            if (!(s2 < P.cut2)) continue;
-            const double inv_d = rsqrt(s2);
-            double sc, sc1d;
-            cubic_sc(P, s2 * inv_d * P.inv_h, inv_d, sc, sc1d);
-            const double cf = (lj + A.lrho[i]) * P.mass * sc;
-            grx -= cf * ex;
-            gry -= cf * ey;
+    // the neighbours the force adjoint recorded, as one flat sequence (cells of
+    // more than 32 particles searched in place), the lanes of a warp together
+    const uint32_t* const masks = G.nbmask + k;
+    const uint32_t over = masks[(size_t)9 * P.n];
+    int c = -1;
+    uint32_t bits = 0, base = 0, next = 0, end = 0;
+    for (;;) {
+        if (bits == 0 && next == end) {
+            for (c++; c < 9; c++) {
+                uint32_t cell;
+                int sx, sy, sz;
+                if (!st.cell(c, cell, sx, sy, sz)) continue;
+                const uint32_t s = G.cell_start[cell];
+                if (s == kEmpty) continue;
+                if ((over >> c) & 1u) {
+                    next = s;
+                    end = G.cell_end[cell];
+                    break;
+                }
+                bits = masks[(size_t)c * P.n];
+                base = s;
+                if (bits) break;
+            }
+            if (c >= 9) break;
         }
+        uint32_t i;
+        bool known;
+        if (bits) {
+            i = base + (uint32_t)(__ffs(bits) - 1);
+            bits &= bits - 1;
+            known = true;
+        } else {
+            i = next++;
+            known = false;
+        }
+        const double ex = __dsub_rn(G.rx[i], xj), ey = __dsub_rn(G.ry[i], yj);
+        const double s2 = exact_dist2<2>(ex, ey, 0.0);
+        if (!known && !(i != k && G.itype[i] != P.type_non_existent && s2 < P.cut2)) continue;
+        const double inv_d = rsqrt(s2);
+        double sc, sc1d;
+        cubic_sc(P, s2 * inv_d * P.inv_h, inv_d, sc, sc1d);
+        const double cf = (lj + A.lrho[i]) * P.mass * sc;
+        grx -= cf * ex;
+        gry -= cf * ey;
     }
     A.out_rx[id] += grx;
     A.out_ry[id] += gry;
@@ -487,7 +574,8 @@ void enqueue_reverse_step(rrsph_solver* s, AdjointRun* run, uint64_t m, size_t j
     const double v_dt = (run->step0 + m) ? run->dt : run->dt * 0.5;
     const unsigned blocks = (unsigned)((n + 255) / 256);
     const unsigned gblocks = (unsigned)((n + rrsph::kAdjThreads - 1) / rrsph::kAdjThreads);
-    rrsph::k_adj_reorder<<<blocks, 256, 0, st>>>(s->P, s->G, sv, run->seg_rho + j * n, A, run->dt, v_dt, piston);
+    rrsph::k_adj_reorder<<<blocks, 256, 0, st>>>(s->P, s->G, sv, run->seg_rho + j * n, s->S.coff2, A, run->dt, v_dt,
+                                                 piston);
     rrsph::k_adj_forces<<<gblocks, rrsph::kAdjThreads, 0, st>>>(s->P, s->G, A, run->dt);
     rrsph::k_adj_density<<<gblocks, rrsph::kAdjThreads, 0, st>>>(s->P, s->G, A);
     s->launches += 4;
