@@ -423,6 +423,53 @@ def test_out_of_domain_is_an_error(gpu_available):
         assert s.status() & capi.FLAG_OUT_OF_DOMAIN
 
 
+@pytest.mark.parametrize("treatment", [0, 1])
+def test_fp64_cells_of_more_than_32_particles_vs_oracle(gpu_available, treatment):
+    """A dense patch of boundary particles (a third of the lattice spacing, in
+    an empty corner of the tank) puts more than 32 particles into some cells;
+    the FP64 gathers search those cells in place, in the search's order. Pairs
+    of every step, the state after three steps and the last step's
+    accelerations (fluid and patch apart) against the oracle."""
+    import dataclasses
+
+    from oracle import binding as O
+    from sph2d_gb300 import Solver
+
+    base = _dam(nx=40, ny=20, density_treatment=treatment)
+    dx = float(base.particle["delta"])
+    g = (np.arange(12) + 0.5) * dx / 3.0
+    gx, gy = np.meshgrid(g, g, indexing="ij")
+    patch = np.stack([2.5 + gx.ravel(), 1.0 + gy.ravel()], axis=1)
+    m = len(patch)
+    case = dataclasses.replace(
+        base,
+        r=np.concatenate([base.r, patch]),
+        v=np.zeros((base.ntotal + m, 2)),
+        rho=np.concatenate([base.rho, np.full(m, 1000.0)]),
+        itype=np.concatenate([base.itype, np.full(m, base.itype[-1])]).astype(np.int32),
+        particle=dict(base.particle, ntotal=base.ntotal + m, nvirt=int(base.particle["nvirt"]) + m),
+        model=dict(base.model, max_neighbours=512),
+    )
+    p = case.params()
+    ref = O.run(p, case.r, case.v, case.rho, case.itype, nsteps=3)
+    with Solver(p, "fp64") as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        keys, _, _ = s.grid_find()
+        assert np.bincount(keys).max() > 32
+        pairs = []
+        t = 0.0
+        for _ in range(3):
+            t = s.step(1, t)
+            pairs.append(s.pair_count()[0])
+        st = s.download()
+        a = s.download_rates()["a"]
+    assert pairs == [int(x) for x in ref["pairs_each"]]
+    for key in ("r", "v", "rho", "p"):
+        assert rel_l2(st[key], ref[key]) < 1e-10, key
+    assert rel_l2(a[:-m], ref["a"][:-m]) < 1e-10
+    assert rel_l2(a[-m:], ref["a"][-m:]) < 1e-10
+
+
 def test_neighbour_overflow_is_an_error(gpu_available):
     from oracle import binding as O
     from sph2d_gb300 import RrsphError, Solver, capi
