@@ -65,10 +65,10 @@ struct Sorted {
     float4* VD4n;
     // Neighbour masks written by the density pass for the force pass (the FP64
     // step, 2D and 3D; the 2D mixed step without reuse), SoA [NC + 1][n] with
-    // NC = 3^dim stencil cells: word c < NC = bit b set if particle
-    // cell_start + b of stencil cell c is a neighbour; word NC = stencil cells
-    // with more than 32 particles (searched again by the force pass). Null
-    // where unused.
+    // NC = 3^dim stencil cells, of 32-bit words (64-bit in the 3D FP64 step):
+    // word c < NC = bit b set if particle cell_start + b of stencil cell c is a
+    // neighbour; word NC = stencil cells with more particles than a word has
+    // bits (searched again by the force pass). Null where unused.
     uint32_t* nbmask;
     // mixed step with neighbour reuse: up to kVerletCap2 (2D) / kVerletCap3 (3D)
     // candidates per particle, sorted index | cell code << 27 (3D: << 25) with

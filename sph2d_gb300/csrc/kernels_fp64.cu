@@ -3,6 +3,8 @@
 // particle are the particles of the 3^dim cells around its cell that pass the
 // reference's cutoff test, visited in the reference's order (cells x-major,
 // ids ascending inside a cell), so the sums run in the same order as RRSPH_OMP.
+#include <type_traits>
+
 #include "kernels.cuh"
 #include "neighbour.cuh"
 
@@ -21,6 +23,19 @@ __device__ __forceinline__ void warp_max_bits(unsigned long long* dst, double v)
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xFFFFFFFFu, v, o));
     if ((threadIdx.x & 31) == 0 && v > 0) atomicMax(dst, dbits(v));
 }
+
+// The neighbour masks of the FP64 gathers: a bit per particle of a stencil
+// cell, 32-bit in 2D and 64-bit in 3D (a 3D cell near a wall holds up to ~40
+// particles); a cell with more is searched in place.
+template <int DIM>
+struct NbMask {
+    using T = typename std::conditional<DIM == 3, unsigned long long, uint32_t>::type;
+    static constexpr uint32_t bits = DIM == 3 ? 64 : 32;
+    static __device__ __forceinline__ T* at(const Sorted& G, uint32_t k) { return reinterpret_cast<T*>(G.nbmask) + k; }
+    static __device__ __forceinline__ uint32_t lowest(T m) {
+        return DIM == 3 ? (uint32_t)(__ffsll((long long)m) - 1) : (uint32_t)(__ffs((int)m) - 1);
+    }
+};
 
 // density_sum (RRSPH_COMMON/include/Density.h:25-61) and density_con
 // (Density.h:63-114, delta-SPH when density_treatment == 2), EOS p (EOS.cpp:31-34).
@@ -48,23 +63,24 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density(DevParams P, Stat
         if (G.itype[k] != P.type_non_existent) {
             const Stencil<DIM> st(P, G.key[k]);
             constexpr int NC = DIM == 3 ? 27 : 9;
-            uint32_t* const masks = G.nbmask + k;  // [c * n]: this particle's bits of stencil cell c
+            using Mask = typename NbMask<DIM>::T;
+            Mask* const masks = NbMask<DIM>::at(G, k);  // [c * n]: this particle's bits of stencil cell c
             const float4 pj4 = G.P4[k];
             const float cellf = P.mf.cell, cut2_hi = P.mf.cut2_hi;
             // 1. The float test on the cell-relative offsets: a particle beyond the
             // cutoff's upper guard band is beyond the cutoff in double too; the
             // others are candidates (bit b of cell c: particle cell_start + b). A cell
-            // of more than 32 particles is searched in place below. The warp goes
-            // through the cells together, so the mask stores are coalesced.
+            // of more particles than a mask has bits is searched in place below. The
+            // warp goes through the cells together, so the mask stores are coalesced.
             uint32_t over = 0;
 #pragma unroll 1
             for (int c = 0; c < NC; c++) {
-                uint32_t cand = 0;
+                Mask cand = 0;
                 uint32_t cell;
                 int sx, sy, sz;
                 const uint32_t s = st.cell(c, cell, sx, sy, sz) ? G.cell_start[cell] : kEmpty;
                 const uint32_t e = s != kEmpty ? G.cell_end[cell] : s;
-                if (e - s > 32) {
+                if (e - s > NbMask<DIM>::bits) {
                     over |= 1u << c;
                 } else {
                     const float shx = (float)sx * cellf - pj4.x, shy = (float)sy * cellf - pj4.y;
@@ -74,20 +90,21 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density(DevParams P, Stat
                         const float fx = pi4.x + shx, fy = pi4.y + shy, fz = DIM == 3 ? pi4.z + shz : 0.0f;
                         const bool cnd = i != k && __float_as_int(pi4.w) != P.type_non_existent &&
                                          fx * fx + fy * fy + fz * fz < cut2_hi;
-                        cand |= (cnd ? 1u : 0u) << (i - s);
+                        cand |= (Mask)(cnd ? 1u : 0u) << (i - s);
                     }
                 }
                 masks[(size_t)c * P.n] = cand;
             }
-            masks[(size_t)NC * P.n] = over;
+            masks[(size_t)NC * P.n] = (Mask)over;
             // 2. The candidates in the search's order (cells in stencil order, ids
             // ascending) as one flat sequence, so the lanes of a warp run the double
             // test and terms together (a warp's FP64 instruction costs the pipe the
             // same time whatever lanes are active). A cell's neighbours replace its
             // candidates in the masks the force pass reads.
             int c = -1;
-            uint32_t bits = 0, base = 0, kept = 0;  // candidates left in a masked cell, and its neighbours
-            uint32_t next = 0, end = 0;             // or the range of a searched cell left
+            Mask bits = 0, kept = 0;     // candidates left in a masked cell, and its neighbours
+            uint32_t base = 0;
+            uint32_t next = 0, end = 0;  // or the range of a searched cell left
             bool masked = false;
             for (;;) {
                 if (bits == 0 && next == end) {
@@ -116,7 +133,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density(DevParams P, Stat
                 uint32_t i, b = 0;
                 bool searched;
                 if (bits) {
-                    b = (uint32_t)(__ffs(bits) - 1);
+                    b = NbMask<DIM>::lowest(bits);
                     i = base + b;
                     bits &= bits - 1;
                     searched = false;
@@ -130,7 +147,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_density(DevParams P, Stat
                 if (!(d2 < P.cut2)) continue;
                 if (searched && (i == k || G.itype[i] == P.type_non_existent)) continue;
                 cnt++;
-                kept |= (searched ? 0u : 1u) << b;
+                kept |= (Mask)(searched ? 0u : 1u) << b;
                 const double dist = sqrt(d2);
                 const double q = dist * P.inv_h;
                 if (!cont) {
@@ -263,17 +280,19 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_forces(DevParams P, State
         if (tj != P.type_non_existent) {
             const Stencil<DIM> st(P, G.key[k]);
             constexpr int NC = DIM == 3 ? 27 : 9;
-            const uint32_t* const masks = use_masks ? G.nbmask + k : nullptr;
-            const uint32_t over = masks ? masks[(size_t)NC * P.n] : 0xFFFFFFFFu;
+            using Mask = typename NbMask<DIM>::T;
+            const Mask* const masks = use_masks ? NbMask<DIM>::at(G, k) : nullptr;
+            const uint32_t over = masks ? (uint32_t)masks[(size_t)NC * P.n] : 0xFFFFFFFFu;
             // One flat sequence over the stencil cells: each iteration takes this
             // particle's next candidate (the next neighbour the density pass recorded
-            // in a cell, or the next particle of a cell searched in place: more than
-            // 32 particles, or no masks), so the lanes of a warp run the double pair
+            // in a cell, or the next particle of a cell searched in place: more
+            // particles than a mask has bits, or no masks), so the lanes of a warp run the double pair
             // body together (a warp's FP64 instruction costs the pipe the same time
             // whatever lanes are active). The order is the search's: cells in
             // stencil order, ids ascending.
             int c = -1;
-            uint32_t bits = 0, base = 0;  // the recorded neighbours of the current cell
+            Mask bits = 0;                // the recorded neighbours of the current cell
+            uint32_t base = 0;
             uint32_t next = 0, end = 0;   // or the range left to search
             for (;;) {
                 if (bits == 0 && next == end) {
@@ -297,7 +316,7 @@ __global__ void __launch_bounds__(kMaxGatherThreads) k_forces(DevParams P, State
                 uint32_t i;
                 bool known;
                 if (bits) {
-                    i = base + (uint32_t)(__ffs(bits) - 1);
+                    i = base + NbMask<DIM>::lowest(bits);
                     bits &= bits - 1;
                     known = true;
                 } else {

@@ -508,7 +508,8 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
     if (!mixed) {
         A(G.vx, n); A(G.vy, n); if (d3) A(G.vz, n);
         A(G.rho, n); A(G.p, n); A(G.pr2, n);
-        A(G.nbmask, (size_t)(d3 ? 28 : 10) * n);  // the density pass's pairs for the force pass
+        // the density pass's pairs for the force pass: [3^dim + 1][n] masks, 64-bit in 3D
+        A(G.nbmask, (size_t)(d3 ? 2 * 28 : 10) * n);
         // cell-relative float offsets (key pass) and their cell-order copy: the
         // density pass's float test rejects the stencil particles beyond the cutoff
         if (d3) A(S.coff4, n); else A(S.coff2, n);
