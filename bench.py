@@ -329,12 +329,11 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     errors_cont = continuity_rate_error()
 
     # ---- end to end through the C ABI with pinned host buffers: each step is
-    # one call of the drop-in boundary on host arrays (rrsph_upload of the
-    # state, rrsph_step(1), rrsph_download of the new state), and the next step
-    # uploads the state the last one downloaded, so the run advances and its
-    # list rebuilds fall inside the timed region (as the reference's
-    # time_integration would run if called for one step at a time: fresh work
-    # arrays at every call)
+    # one call of the drop-in boundary on host arrays (rrsph_step_host: upload
+    # of the state, one step, download of the new state into the same arrays),
+    # so the run advances and its list rebuilds fall inside the timed region
+    # (as the reference's time_integration would run if called for one step at
+    # a time: fresh work arrays at every call)
     pin = lambda x: torch.from_numpy(np.ascontiguousarray(x)).pin_memory().numpy()  # noqa: E731
     n = case.ntotal
     host = {"r": pin(case.r), "v": pin(case.v), "rho": pin(case.rho), "p": pin(np.zeros(n)),
@@ -349,15 +348,12 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     e2e_time = [0.0]
 
     def e2e_step():
-        # p is not an input of the step (the density pass computes it from rho), as in the reference's loop
-        capi.check(L.rrsph_upload(sm.handle, dp(host["r"]), 2, dp(host["v"]), dp(host["rho"]), None,
-                                  ip(host["itype"])))
+        # r, v, rho, itype in and out; p out only (the density pass computes it from rho), as in the reference's loop
         tt = C.c_double(e2e_time[0])
-        capi.check(L.rrsph_step(sm.handle, 1, C.byref(tt)))
+        capi.check(L.rrsph_step_host(sm.handle, 1, C.byref(tt), dp(host["r"]), 2, dp(host["v"]), dp(host["rho"]),
+                                     dp(host["p"]), ip(host["itype"])))
         e2e_time[0] = tt.value
-        capi.check(L.rrsph_download(sm.handle, dp(host["r"]), 2, dp(host["v"]), dp(host["rho"]), dp(host["p"]),
-                                    ip(host["itype"])))
-        pairs = C.c_uint64()  # the step's pairs, as rrsph_step read them back (no device access)
+        pairs = C.c_uint64()  # the step's pairs, as the call read them back (no device access)
         capi.check(L.rrsph_last_report(sm.handle, None, None, C.byref(pairs), None))
         return pairs.value
 
@@ -458,8 +454,9 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": e2e_steps, "rebuilds": e2e_rebuilds,
                 "ms_per_step_median": statistics.median(e2e_each) * 1e3, "ms_per_step_max": max(e2e_each) * 1e3,
-                "path": "rrsph_upload + rrsph_step(1) + rrsph_download per step on pinned host buffers, each "
-                        "step uploading the state the last one downloaded"},
+                "path": "rrsph_step_host(1) per step on pinned host buffers (upload of r, v, rho, itype, one "
+                        "step, download of r, v, rho, p, itype into the same arrays, one wait), each step "
+                        "uploading the state the last one returned"},
         "gpu_launches": launches,
         "checks": {
             "fluid_mass_exact": diag1["mass"] == diag0["mass"],

@@ -215,6 +215,17 @@ int rrsph_download(rrsph_solver* s, double* r, uint32_t stride, double* v,
  * *time_io is the simulation time before the first step and is advanced.
  * The first step after rrsph_upload uses dt/2 for velocities (WholeStep.cpp:33). */
 int rrsph_step(rrsph_solver* s, uint64_t nsteps, double* time_io);
+/* The drop-in call on host arrays, as the reference's time_integration runs
+ * on its arrays: rrsph_upload(r, stride, v, rho, NULL, itype), rrsph_step(
+ * nsteps, time_io), rrsph_download(r, stride, v, rho, pres, itype), with one
+ * wait at the end. r, v, rho and itype are read, then overwritten with the
+ * state after the steps; pres (may be NULL) receives p. With graph replay, p
+ * (and rho with summation density, which the whole step does not change)
+ * come back while the last step's force gather runs. Page-locked arrays are
+ * read and written over the host link by kernels, as in rrsph_upload and
+ * rrsph_download. */
+int rrsph_step_host(rrsph_solver* s, uint64_t nsteps, double* time_io, double* r, uint32_t stride, double* v,
+                    double* rho, double* pres, int32_t* itype);
 /* Asynchronous form of rrsph_step: enqueues nsteps steps on the handle's
  * stream and returns without waiting. The simulation time continues on the
  * device from the previous step (or from rrsph_set_time). Errors raised by the

@@ -604,14 +604,7 @@ extern "C" int rrsph_set_piston_fourier(rrsph_solver* s, uint32_t ncoef, double 
     if (cudaSetDevice(s->device) != cudaSuccess) return set_error(RRSPH_ERR_CUDA, "rrsph_set_piston_fourier: device");
     // the step graphs hold the parameters by value
     cudaStreamSynchronize(s->stream);
-    for (auto& g : s->graph) {
-        if (g) cudaGraphExecDestroy(g);
-        g = nullptr;
-    }
-    for (auto& g : s->graph_run) {
-        if (g) cudaGraphExecDestroy(g);
-        g = nullptr;
-    }
+    rrsph_impl::destroy_step_graphs(s);
     s->P.fourier_n = (int)ncoef;
     s->P.fourier_omega = ncoef ? omega : 0.0;
     for (int k = 0; k < RRSPH_PISTON_FOURIER_MAX; k++) s->P.fourier_coef[k] = k < (int)ncoef ? coef[k] : 0.0;

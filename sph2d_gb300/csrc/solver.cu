@@ -178,14 +178,7 @@ int key_bits(uint64_t max_cells) {
 
 void drop_graphs(rrsph_solver* s) {
     cudaStreamSynchronize(s->stream);
-    for (auto& g : s->graph) {
-        if (g) cudaGraphExecDestroy(g);
-        g = nullptr;
-    }
-    for (auto& g : s->graph_run) {
-        if (g) cudaGraphExecDestroy(g);
-        g = nullptr;
-    }
+    rrsph_impl::destroy_step_graphs(s);
 }
 
 // Candidate-list cutoff (cell + skin, widened a little: a list may hold more
@@ -352,6 +345,7 @@ int enqueue_step_verlet(rrsph_solver* s, int par, cudaEvent_t* events, bool with
     const bool d3 = s->dim == 3;
     if (d3) rrsph::launch_density_verlet<3>(s->P, s->S, s->G, cur, s->flags, st, s->gather_threads[0]);
     else rrsph::launch_density_verlet<2>(s->P, s->S, s->G, cur, s->flags, st, s->gather_threads[0]);
+    if (s->mark_density) RRSPH_CUDA_TRY(cudaEventRecordWithFlags(s->ev_density, st, cudaEventRecordExternal));
     if (events) cudaEventRecord(events[4], st);
     // the whole step runs inside the force gather unless dt waits for the step's
     // maxima or a particle may have more neighbours than a list holds
@@ -401,6 +395,7 @@ void enqueue_step(rrsph_solver* s, int par, cudaEvent_t* events, bool with_keys)
     rrsph::launch_reorder<DIM>(s->P, s->S, s->G, fsrc, s->precision == RRSPH_PRECISION_MIXED, s->stream);
     if (events) cudaEventRecord(events[3], s->stream);
     enqueue_density<DIM>(s, cur);
+    if (s->mark_density) cudaEventRecordWithFlags(s->ev_density, s->stream, cudaEventRecordExternal);
     if (events) cudaEventRecord(events[4], s->stream);
     enqueue_forces<DIM>(s, RRSPH_TERM_ALL, cur, 0, 1);
     if (events) cudaEventRecord(events[5], s->stream);
@@ -604,10 +599,10 @@ extern "C" void rrsph_destroy(rrsph_solver* s) {
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
     rrsph_impl::adjoint_release(s);
-    for (int i = 0; i < 2; i++) {
-        if (s->graph[i]) cudaGraphExecDestroy(s->graph[i]);
-        if (s->graph_run[i]) cudaGraphExecDestroy(s->graph_run[i]);
-    }
+    rrsph_impl::destroy_step_graphs(s);
+    if (s->ev_density) cudaEventDestroy(s->ev_density);
+    if (s->ev_dl) cudaEventDestroy(s->ev_dl);
+    if (s->dl_stream) cudaStreamDestroy(s->dl_stream);
     for (int i = 0; i <= kPhases; i++)
         if (s->ev[i]) cudaEventDestroy(s->ev[i]);
     for (void* a : s->allocations)
@@ -640,15 +635,13 @@ const void* device_view(const void* host) {
     }
     return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
-int finish_upload(rrsph_solver* s);
-}  // namespace
+int finish_upload(rrsph_solver* s, bool wait);
 
-extern "C" int rrsph_upload(rrsph_solver* s, const double* r, uint32_t stride, const double* v, const double* rho,
-                            const double* pres, const int32_t* itype) {
-    int rc = check_handle(s, "rrsph_upload");
-    if (rc) return rc;
-    if (!r || !v || !rho || !itype) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_upload: null array");
-    if (stride < (uint32_t)s->dim) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_upload: stride < dim");
+// rrsph_upload without the checks; wait: return after the caller's arrays
+// were read (else they are read in stream order).
+int upload_impl(rrsph_solver* s, const double* r, uint32_t stride, const double* v, const double* rho,
+                const double* pres, const int32_t* itype, bool wait) {
+    int rc;
     const size_t n = s->P.n;
     auto& S = s->S;
     cudaStream_t st = s->stream;
@@ -671,7 +664,7 @@ extern "C" int rrsph_upload(rrsph_solver* s, const double* r, uint32_t stride, c
             rrsph::launch_upload_direct<2>(s->P, S, s->G, dr, dv, drho, dp, dit, stride, s->scal, s->params.dt,
                                            s->flags, st);
         s->launches++;
-        RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
+        if (wait) RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
         s->step_index = 0;
         s->nlist_valid = false;
         s->keys_ready = true;  // the upload kernel ran the first step's key pass
@@ -697,13 +690,23 @@ extern "C" int rrsph_upload(rrsph_solver* s, const double* r, uint32_t stride, c
         if (S.avz) RRSPH_CUDA_TRY(cudaMemsetAsync(S.avz, 0, n * sizeof(double), st));
     }
     RRSPH_CUDA_TRY(cudaMemsetAsync(S.drho, 0, n * sizeof(double), st));
-    return finish_upload(s);
+    return finish_upload(s, wait);
+}
+}  // namespace
+
+extern "C" int rrsph_upload(rrsph_solver* s, const double* r, uint32_t stride, const double* v, const double* rho,
+                            const double* pres, const int32_t* itype) {
+    int rc = check_handle(s, "rrsph_upload");
+    if (rc) return rc;
+    if (!r || !v || !rho || !itype) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_upload: null array");
+    if (stride < (uint32_t)s->dim) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_upload: stride < dim");
+    return upload_impl(s, r, stride, v, rho, pres, itype, true);
 }
 
 namespace {
 // The rest of rrsph_upload after the state is on the device: the step
-// scalars, the neighbour-list check, and the wait for the caller's arrays.
-int finish_upload(rrsph_solver* s) {
+// scalars, the neighbour-list check, and (wait) the wait for the caller's arrays.
+int finish_upload(rrsph_solver* s, bool wait) {
     auto& S = s->S;
     cudaStream_t st = s->stream;
     rrsph::StepScalars init{};
@@ -714,7 +717,7 @@ int finish_upload(rrsph_solver* s) {
         rrsph::launch_verlet_upload_check(S.vl_rebuild, S.vl_gone, st);
         s->launches++;
     }
-    RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
+    if (wait) RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
     s->step_index = 0;
     s->nlist_valid = false;
     s->keys_ready = false;
@@ -722,11 +725,11 @@ int finish_upload(rrsph_solver* s) {
 }
 }  // namespace
 
-extern "C" int rrsph_download(rrsph_solver* s, double* r, uint32_t stride, double* v, double* rho, double* pres,
-                              int32_t* itype) {
-    int rc = check_handle(s, "rrsph_download");
-    if (rc) return rc;
-    if ((r || v) && stride < (uint32_t)s->dim) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_download: stride < dim");
+namespace {
+// rrsph_download without the checks; wait: return after the arrays were written.
+int download_impl(rrsph_solver* s, double* r, uint32_t stride, double* v, double* rho, double* pres, int32_t* itype,
+                  bool wait) {
+    int rc;
     const size_t n = s->P.n;
     cudaStream_t st = s->stream;
     // page-locked caller arrays: one kernel writes them over the host link
@@ -739,7 +742,7 @@ extern "C" int rrsph_download(rrsph_solver* s, double* r, uint32_t stride, doubl
         if (s->dim == 3) rrsph::launch_download_direct<3>(s->P, s->S, dr, dv, drho, dp, dit, stride, st);
         else rrsph::launch_download_direct<2>(s->P, s->S, dr, dv, drho, dp, dit, stride, st);
         s->launches++;
-        RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
+        if (wait) RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
         return RRSPH_OK;
     }
     if (r || v) {
@@ -753,8 +756,17 @@ extern "C" int rrsph_download(rrsph_solver* s, double* r, uint32_t stride, doubl
     if (rho) RRSPH_CUDA_TRY(cudaMemcpyAsync(rho, s->S.rho, n * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (pres) RRSPH_CUDA_TRY(cudaMemcpyAsync(pres, s->S.p, n * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (itype) RRSPH_CUDA_TRY(cudaMemcpyAsync(itype, s->S.itype, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-    RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
+    if (wait) RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
     return RRSPH_OK;
+}
+}  // namespace
+
+extern "C" int rrsph_download(rrsph_solver* s, double* r, uint32_t stride, double* v, double* rho, double* pres,
+                              int32_t* itype) {
+    int rc = check_handle(s, "rrsph_download");
+    if (rc) return rc;
+    if ((r || v) && stride < (uint32_t)s->dim) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_download: stride < dim");
+    return download_impl(s, r, stride, v, rho, pres, itype, true);
 }
 
 namespace {
@@ -810,7 +822,9 @@ int ensure_graphs(rrsph_solver* s) {
     return RRSPH_OK;
 }
 
-int enqueue_steps(rrsph_solver* s, uint64_t nsteps) {
+// nsteps steps on the handle's stream; mark_last: the last step records
+// ev_density after its density pass (graph replay only).
+int enqueue_steps(rrsph_solver* s, uint64_t nsteps, bool mark_last = false) {
     cudaStream_t st = s->stream;
     for (uint64_t k = 0; k < nsteps;) {
         const int par = (int)(s->step_index & 1);
@@ -832,10 +846,19 @@ int enqueue_steps(rrsph_solver* s, uint64_t nsteps) {
             if (rc) return rc;
             if (with_keys) enqueue_keys_dim(s, par);
             // whole runs of kRunSteps steps as one graph launch, the rest one step each
-            if (nsteps - k >= (uint64_t)kRunSteps) {
+            if (nsteps - k - (mark_last ? 1 : 0) >= (uint64_t)kRunSteps) {
                 RRSPH_CUDA_TRY(cudaGraphLaunch(s->graph_run[par], st));
                 s->launches += s->launches_in_run[par];
                 done = kRunSteps;
+            } else if (mark_last && k + 1 == nsteps) {
+                if (!s->graph_mark[par]) {
+                    s->mark_density = true;
+                    const int rm = capture_steps(s, par, 1, &s->graph_mark[par], &s->launches_in_mark[par]);
+                    s->mark_density = false;
+                    if (rm) return rm;
+                }
+                RRSPH_CUDA_TRY(cudaGraphLaunch(s->graph_mark[par], st));
+                s->launches += s->launches_in_mark[par];
             } else {
                 RRSPH_CUDA_TRY(cudaGraphLaunch(s->graph[par], st));
                 s->launches += s->launches_in_graph[par];
@@ -890,6 +913,44 @@ extern "C" int rrsph_step(rrsph_solver* s, uint64_t nsteps, double* time_io) {
     RRSPH_CUDA_TRY(cudaGetLastError());
     s->launches++;
     if ((rc = enqueue_steps(s, nsteps)) != 0) return rc;
+    return rrsph_sync(s, time_io);
+}
+
+extern "C" int rrsph_step_host(rrsph_solver* s, uint64_t nsteps, double* time_io, double* r, uint32_t stride,
+                               double* v, double* rho, double* pres, int32_t* itype) {
+    int rc = check_handle(s, "rrsph_step_host");
+    if (rc) return rc;
+    if (!time_io || !r || !v || !rho || !itype) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_step_host: null argument");
+    if (stride < (uint32_t)s->dim) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_step_host: stride < dim");
+    if (nsteps == 0) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_step_host: no steps");
+    cudaStream_t st = s->stream;
+    const size_t n = s->P.n;
+    // with graph replay the last step marks the end of its density pass: p, and
+    // rho with summation density (the whole step leaves it), come back on a
+    // copy stream while the force gather runs
+    const bool mark = s->graphs && !s->timing;
+    if (mark && !s->dl_stream) {
+        if (cudaStreamCreateWithFlags(&s->dl_stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s->ev_density, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s->ev_dl, cudaEventDisableTiming) != cudaSuccess)
+            return set_error(RRSPH_ERR_CUDA, "rrsph_step_host: copy stream");
+    }
+    if ((rc = upload_impl(s, r, stride, v, rho, nullptr, itype, false)) != 0) return rc;
+    rrsph::launch_set_time(&s->scal[s->step_index & 1], *time_io, s->flags, st);  // time, flags cleared
+    RRSPH_CUDA_TRY(cudaGetLastError());
+    s->launches++;
+    if ((rc = enqueue_steps(s, nsteps, mark)) != 0) return rc;
+    const bool early_rho = mark && s->P.density_treatment == 0;
+    if (mark) {
+        RRSPH_CUDA_TRY(cudaStreamWaitEvent(s->dl_stream, s->ev_density, 0));
+        if (pres) RRSPH_CUDA_TRY(cudaMemcpyAsync(pres, s->S.p, n * sizeof(double), cudaMemcpyDeviceToHost, s->dl_stream));
+        if (early_rho)
+            RRSPH_CUDA_TRY(cudaMemcpyAsync(rho, s->S.rho, n * sizeof(double), cudaMemcpyDeviceToHost, s->dl_stream));
+        RRSPH_CUDA_TRY(cudaEventRecord(s->ev_dl, s->dl_stream));
+    }
+    if ((rc = download_impl(s, r, stride, v, early_rho ? nullptr : rho, mark ? nullptr : pres, itype, false)) != 0)
+        return rc;
+    if (mark) RRSPH_CUDA_TRY(cudaStreamWaitEvent(st, s->ev_dl, 0));
     return rrsph_sync(s, time_io);
 }
 

@@ -56,9 +56,17 @@ struct rrsph_solver {
     bool graphs = true;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};      // one step, starting at parity 0 / 1
     cudaGraphExec_t graph_run[2] = {nullptr, nullptr};  // kRunSteps steps, starting at parity 0 / 1
+    cudaGraphExec_t graph_mark[2] = {nullptr, nullptr}; // one step recording ev_density after its density pass
     unsigned long long launches = 0;
     unsigned long long launches_in_graph[2] = {0, 0};
     unsigned long long launches_in_run[2] = {0, 0};
+    unsigned long long launches_in_mark[2] = {0, 0};
+    // rrsph_step_host: the copy stream that brings back what the last density
+    // pass finished while the force gather runs, and its events
+    cudaStream_t dl_stream = nullptr;
+    cudaEvent_t ev_density = nullptr;  // recorded (external) after the marked step's density pass
+    cudaEvent_t ev_dl = nullptr;       // the copy stream's work done
+    bool mark_density = false;         // capturing: record ev_density after the density launch
     uint64_t step_index = 0;
     bool keys_ready = false;  // the next step's predict + keys were computed by the last whole step
     bool timing = false;
@@ -91,3 +99,15 @@ void adjoint_release(rrsph_solver* s);
 int flags_status(const rrsph_solver* s, uint32_t f);
 }  // namespace rrsph_impl
 
+
+namespace rrsph_impl {
+// Every captured step graph (the caller synchronises the stream first).
+inline void destroy_step_graphs(rrsph_solver* s) {
+    for (cudaGraphExec_t* set : {s->graph, s->graph_run, s->graph_mark}) {
+        for (int i = 0; i < 2; i++) {
+            if (set[i]) cudaGraphExecDestroy(set[i]);
+            set[i] = nullptr;
+        }
+    }
+}
+}  // namespace rrsph_impl

@@ -143,6 +143,22 @@ class Solver:
         check(lib().rrsph_download(self._h, _dp(r), self.dim, _dp(v), _dp(rho), _dp(pres), _i32p(itype)))
         return {"r": r, "v": v, "rho": rho, "p": pres, "itype": itype}
 
+    def step_host(self, state: dict, nsteps: int = 1, time: float = 0.0) -> float:
+        """rrsph_step_host on a host state dict (r, v, rho, itype; p written
+        if present): upload, nsteps steps and download in one call, in place.
+        The arrays must be C-contiguous float64 (itype int32) with r and v of
+        shape (n, stride >= dim). Returns the time after the steps."""
+        r, v, rho, itype = state["r"], state["v"], state["rho"], state["itype"]
+        pres = state.get("p")
+        for a in (r, v, rho) + (() if pres is None else (pres,)):
+            assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+        assert itype.dtype == np.int32 and itype.flags["C_CONTIGUOUS"]
+        assert r.shape == (self.n, r.shape[1]) and r.shape[1] >= self.dim and v.shape == r.shape
+        t = C.c_double(time)
+        check(lib().rrsph_step_host(self._h, nsteps, C.byref(t), _dp(r), r.shape[1], _dp(v), _dp(rho), _dp(pres),
+                                    _i32p(itype)))
+        return t.value
+
     def download_rates(self) -> dict:
         """Accelerations and drho of the last completed step (rrsph_download_rates)."""
         a = np.zeros((self.n, self.dim))

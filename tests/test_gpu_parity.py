@@ -766,6 +766,48 @@ def test_neighbour_reuse_across_uploads(gpu_available):
         assert np.array_equal(back[k], ref1[k]), k
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("treatment", [0, 1])
+@pytest.mark.parametrize("pinned", [False, True])
+def test_step_host_equals_upload_step_download(gpu_available, precision, treatment, pinned):
+    """rrsph_step_host (one call, p and rho brought back during the last force
+    gather) against rrsph_upload + rrsph_step + rrsph_download, bitwise, over
+    calls of 1, 13 (a ten-step graph, then the marked last step) and 2 steps."""
+    import torch
+
+    from sph2d_gb300 import Solver
+
+    case = _dam(nx=50, ny=25, density_treatment=treatment)
+    p = case.params()
+    chunks = (1, 13, 2)
+    ref = []
+    with Solver(p, precision) as s:
+        st = {"r": case.r, "v": case.v, "rho": case.rho, "itype": case.itype}
+        t = 0.0
+        for n in chunks:
+            s.upload(st["r"], st["v"], st["rho"], st["itype"])
+            t = s.step(n, t)
+            st = s.download()
+            ref.append((st, t, s.pair_count()))
+
+    def buf(a):
+        a = np.ascontiguousarray(a)
+        return torch.from_numpy(a).pin_memory().numpy() if pinned else a.copy()
+
+    h = {"r": buf(case.r), "v": buf(case.v), "rho": buf(case.rho), "itype": buf(case.itype.astype(np.int32)),
+         "p": buf(np.zeros(case.ntotal))}
+    with Solver(p, precision) as s:
+        t = 0.0
+        for j, n in enumerate(chunks):
+            t = s.step_host(h, n, t)
+            exp, te, pairs = ref[j]
+            assert t == te, j
+            for k in ("r", "v", "rho", "p", "itype"):
+                assert np.array_equal(h[k], exp[k]), (j, k)
+            rep = s.last_report()
+            assert (rep["pairs_last"], rep["pairs_total"]) == pairs and rep["time"] == t
+
+
 def test_pinned_host_arrays_upload_and_download_directly(gpu_available):
     """Page-locked caller arrays go through one kernel each way (read and
     written over the host link); the state equals that of pageable arrays,
