@@ -226,6 +226,13 @@ int rrsph_step(rrsph_solver* s, uint64_t nsteps, double* time_io);
  * rrsph_download. */
 int rrsph_step_host(rrsph_solver* s, uint64_t nsteps, double* time_io, double* r, uint32_t stride, double* v,
                     double* rho, double* pres, int32_t* itype);
+/* rrsph_step(nsteps, time_io) then rrsph_download(r, stride, v, rho, pres,
+ * itype) with one wait, the state staying on the device (any array may be
+ * NULL), and p / rho brought back during the last force gather as in
+ * rrsph_step_host: the per-step call of a loop that hands the host arrays to
+ * its output after every step. */
+int rrsph_step_download(rrsph_solver* s, uint64_t nsteps, double* time_io, double* r, uint32_t stride, double* v,
+                        double* rho, double* pres, int32_t* itype);
 /* Asynchronous form of rrsph_step: enqueues nsteps steps on the handle's
  * stream and returns without waiting. The simulation time continues on the
  * device from the previous step (or from rrsph_set_time). Errors raised by the

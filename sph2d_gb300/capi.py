@@ -181,6 +181,7 @@ _SIGS = {
     "rrsph_get_dt": (C.c_int, [C.c_void_p, _dp]),
     "rrsph_pair_count": (C.c_int, [C.c_void_p, _P(C.c_uint64), _P(C.c_uint64)]),
     "rrsph_step_host": (C.c_int, [C.c_void_p, C.c_uint64, _P(C.c_double), _dp, C.c_uint32, _dp, _dp, _dp, _i32p]),
+    "rrsph_step_download": (C.c_int, [C.c_void_p, C.c_uint64, _P(C.c_double), _dp, C.c_uint32, _dp, _dp, _dp, _i32p]),
     "rrsph_last_report": (C.c_int, [C.c_void_p, _P(C.c_double), _P(C.c_uint32), _P(C.c_uint64), _P(C.c_uint64)]),
     "rrsph_grid_find": (C.c_int, [C.c_void_p, _u32p, _u32p, _u32p]),
     "rrsph_neighbours": (C.c_int, [C.c_void_p, _u32p, _u32p, C.c_uint32, _P(C.c_uint64)]),

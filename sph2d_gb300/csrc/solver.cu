@@ -916,13 +916,12 @@ extern "C" int rrsph_step(rrsph_solver* s, uint64_t nsteps, double* time_io) {
     return rrsph_sync(s, time_io);
 }
 
-extern "C" int rrsph_step_host(rrsph_solver* s, uint64_t nsteps, double* time_io, double* r, uint32_t stride,
-                               double* v, double* rho, double* pres, int32_t* itype) {
-    int rc = check_handle(s, "rrsph_step_host");
-    if (rc) return rc;
-    if (!time_io || !r || !v || !rho || !itype) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_step_host: null argument");
-    if (stride < (uint32_t)s->dim) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_step_host: stride < dim");
-    if (nsteps == 0) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_step_host: no steps");
+namespace {
+// rrsph_step_host (upload first) and rrsph_step_download (the state on the
+// device); the arguments are checked by the callers.
+int steps_and_download(rrsph_solver* s, uint64_t nsteps, double* time_io, double* r, uint32_t stride, double* v,
+                       double* rho, double* pres, int32_t* itype, bool upload) {
+    int rc;
     cudaStream_t st = s->stream;
     const size_t n = s->P.n;
     // with graph replay the last step marks the end of its density pass: p, and
@@ -935,12 +934,12 @@ extern "C" int rrsph_step_host(rrsph_solver* s, uint64_t nsteps, double* time_io
             cudaEventCreateWithFlags(&s->ev_dl, cudaEventDisableTiming) != cudaSuccess)
             return set_error(RRSPH_ERR_CUDA, "rrsph_step_host: copy stream");
     }
-    if ((rc = upload_impl(s, r, stride, v, rho, nullptr, itype, false)) != 0) return rc;
+    if (upload && (rc = upload_impl(s, r, stride, v, rho, nullptr, itype, false)) != 0) return rc;
     rrsph::launch_set_time(&s->scal[s->step_index & 1], *time_io, s->flags, st);  // time, flags cleared
     RRSPH_CUDA_TRY(cudaGetLastError());
     s->launches++;
     if ((rc = enqueue_steps(s, nsteps, mark)) != 0) return rc;
-    const bool early_rho = mark && s->P.density_treatment == 0;
+    const bool early_rho = mark && rho && s->P.density_treatment == 0;
     if (mark) {
         RRSPH_CUDA_TRY(cudaStreamWaitEvent(s->dl_stream, s->ev_density, 0));
         if (pres) RRSPH_CUDA_TRY(cudaMemcpyAsync(pres, s->S.p, n * sizeof(double), cudaMemcpyDeviceToHost, s->dl_stream));
@@ -952,6 +951,27 @@ extern "C" int rrsph_step_host(rrsph_solver* s, uint64_t nsteps, double* time_io
         return rc;
     if (mark) RRSPH_CUDA_TRY(cudaStreamWaitEvent(st, s->ev_dl, 0));
     return rrsph_sync(s, time_io);
+}
+}  // namespace
+
+extern "C" int rrsph_step_host(rrsph_solver* s, uint64_t nsteps, double* time_io, double* r, uint32_t stride,
+                               double* v, double* rho, double* pres, int32_t* itype) {
+    int rc = check_handle(s, "rrsph_step_host");
+    if (rc) return rc;
+    if (!time_io || !r || !v || !rho || !itype) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_step_host: null argument");
+    if (stride < (uint32_t)s->dim) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_step_host: stride < dim");
+    if (nsteps == 0) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_step_host: no steps");
+    return steps_and_download(s, nsteps, time_io, r, stride, v, rho, pres, itype, true);
+}
+
+extern "C" int rrsph_step_download(rrsph_solver* s, uint64_t nsteps, double* time_io, double* r, uint32_t stride,
+                                   double* v, double* rho, double* pres, int32_t* itype) {
+    int rc = check_handle(s, "rrsph_step_download");
+    if (rc) return rc;
+    if (!time_io) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_step_download: null time");
+    if ((r || v) && stride < (uint32_t)s->dim) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_step_download: stride < dim");
+    if (nsteps == 0) return set_error(RRSPH_ERR_INVALID_ARGUMENT, "rrsph_step_download: no steps");
+    return steps_and_download(s, nsteps, time_io, r, stride, v, rho, pres, itype, false);
 }
 
 extern "C" int rrsph_last_report(rrsph_solver* s, double* time, uint32_t* flags, uint64_t* pairs_last,

@@ -7,9 +7,9 @@
 // The reference's loop (TimeIntegration.cpp:21-102) allocates its work arrays,
 // runs predict / grid / density / forces / whole step per step and hands the
 // host arrays to RRSPHOutput::update_step after each step. Here the state lives
-// on the GPU for the whole run: one rrsph_step per step (the loop body, with
-// the piston call the OpenMP loop leaves commented out enabled, as the OpenCL
-// backend has it), then a download into the caller's arrays so that
+// on the GPU for the whole run: one rrsph_step_download per step (the loop
+// body, with the piston call the OpenMP loop leaves commented out enabled, as
+// the OpenCL backend has it, and the download into the caller's arrays) so that
 // update_step writes its data and dump layers and runs its boundary check from
 // host copies exactly as it does for RRSPH_OMP. A step whose device check
 // fails still downloads first, so update_step writes the crash dump and throws
@@ -78,9 +78,10 @@ void time_integration(vheap_darray_floatn& r_var, vheap_darray_floatn& v_var, he
     rr_uint itimestep = 0;
     while (time <= params.simulation_time) {
         RRSPHOutput::instance().start_step(time);
-        const int rc = rrsph_step(h.s, 1, &time);  // time += dt (also when the step's check fails)
+        // the step and the download of its state (time += dt also when the step's check fails)
+        const int rc = rrsph_step_download(h.s, 1, &time, r, stride, v, &rho(0), &p(0), it.data());
         const std::string step_error = rc == RRSPH_OK ? std::string() : rrsph_last_error();
-        ok(rrsph_download(h.s, r, stride, v, &rho(0), &p(0), it.data()));
+        if (rc != RRSPH_OK) ok(rrsph_download(h.s, r, stride, v, &rho(0), &p(0), it.data()));
         for (rr_uint i = 0; i < n; ++i) itype(i) = it[i];
         itimestep++;
         RRSPHOutput::instance().update_step(time, itimestep);  // layers; its check throws on a failed step

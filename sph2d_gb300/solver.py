@@ -159,6 +159,19 @@ class Solver:
                                     _i32p(itype)))
         return t.value
 
+    def step_download(self, nsteps: int = 1, time: float = 0.0):
+        """rrsph_step_download: nsteps steps and the download of the state in one
+        call. Returns (time, state dict as download())."""
+        r = np.zeros((self.n, self.dim))
+        v = np.zeros((self.n, self.dim))
+        rho = np.zeros(self.n)
+        pres = np.zeros(self.n)
+        itype = np.zeros(self.n, dtype=np.int32)
+        t = C.c_double(time)
+        check(lib().rrsph_step_download(self._h, nsteps, C.byref(t), _dp(r), self.dim, _dp(v), _dp(rho), _dp(pres),
+                                        _i32p(itype)))
+        return t.value, {"r": r, "v": v, "rho": rho, "p": pres, "itype": itype}
+
     def download_rates(self) -> dict:
         """Accelerations and drho of the last completed step (rrsph_download_rates)."""
         a = np.zeros((self.n, self.dim))

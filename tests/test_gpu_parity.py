@@ -808,6 +808,32 @@ def test_step_host_equals_upload_step_download(gpu_available, precision, treatme
             assert (rep["pairs_last"], rep["pairs_total"]) == pairs and rep["time"] == t
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("treatment", [0, 1])
+def test_step_download_equals_step_then_download(gpu_available, precision, treatment):
+    """rrsph_step_download (the state staying on the device) against rrsph_step
+    + rrsph_download, bitwise, over calls of 1 and 12 steps."""
+    from sph2d_gb300 import Solver
+
+    case = _dam(nx=50, ny=25, density_treatment=treatment)
+    p = case.params()
+    ref = []
+    with Solver(p, precision) as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        t = 0.0
+        for n in (1, 12):
+            t = s.step(n, t)
+            ref.append((t, s.download()))
+    with Solver(p, precision) as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        t = 0.0
+        for j, n in enumerate((1, 12)):
+            t, st = s.step_download(n, t)
+            assert t == ref[j][0]
+            for k in ("r", "v", "rho", "p", "itype"):
+                assert np.array_equal(st[k], ref[j][1][k]), (j, k)
+
+
 def test_pinned_host_arrays_upload_and_download_directly(gpu_available):
     """Page-locked caller arrays go through one kernel each way (read and
     written over the host link); the state equals that of pageable arrays,
