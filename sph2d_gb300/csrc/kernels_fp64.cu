@@ -3,6 +3,10 @@
 // particle are the particles of the 3^dim cells around its cell that pass the
 // reference's cutoff test, visited in the reference's order (cells x-major,
 // ids ascending inside a cell), so the sums run in the same order as RRSPH_OMP.
+// The density pass records them per stencil cell as bit masks for the force
+// pass, and both walk a particle's pairs as one flat sequence across the cells
+// so that the lanes of a warp run the double pair body together: a warp's FP64
+// instruction costs the pipe the same time whatever lanes are active.
 #include <type_traits>
 
 #include "kernels.cuh"
