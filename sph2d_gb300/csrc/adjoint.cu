@@ -17,7 +17,9 @@
 // from i, so every particle gathers ∂ℓ/∂(its own r, v*, rho, p) over its
 // neighbours and no pair result is scattered (no atomics). The density part is
 // ℓ_rho = (λrho_j + λrho_i) m W(|e|), gathered the same way. The neighbour
-// pairs of step n are those of the forward step, found again from r^n.
+// pairs of step n are the forward step's own: its sorted grid (keys, ids) and
+// the neighbour masks its density pass recorded are kept for every step of the
+// segment being reversed.
 //
 // Checkpointing: the forward run stores S^n every K steps; the reverse sweep
 // takes the segments last to first, recomputes the K states of a segment from
@@ -121,8 +123,8 @@ __global__ void k_gauge_arg(uint32_t n, const double* __restrict__ rx, const dou
 // Cell-order copies of step n's forward quantities (the grid of r^n), and the
 // adjoint of whole_step and the piston: from the adjoints of S^{n+1} to those
 // before the step's updates, and λa of step n in cell order.
-__global__ void k_adj_reorder(DevParams P, Sorted G, SnapView sn, const double* __restrict__ rho_n,
-                              const float2* __restrict__ coff, AdjBuf A, double dt, double v_dt, int piston) {
+__global__ void k_adj_reorder(DevParams P, Sorted G, SnapView sn, const double* __restrict__ rho_n, AdjBuf A,
+                              double dt, double v_dt, int piston) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= P.n) return;
     const uint32_t key = G.key[k];
@@ -139,8 +141,6 @@ __global__ void k_adj_reorder(DevParams P, Sorted G, SnapView sn, const double* 
     G.rho[k] = rho;
     G.p[k] = p;
     G.itype[k] = t;
-    const float2 o = coff[id];  // the key pass's cell-relative offsets of r^n (the float first test)
-    G.P4[k] = make_float4(o.x, o.y, 0.0f, __int_as_float(t));
     A.pr2[k] = p / (rho * rho);
     double lrx = A.in_rx[id], lry = A.in_ry[id], lvx = A.in_vx[id], lvy = A.in_vy[id];
     double lax = A.in_ax[id], lay = A.in_ay[id];
@@ -181,84 +181,47 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_forces(DevParams P, Sorted 
         const double m = P.mass;
         const double ac = P.av_alpha * P.c_av;
         const bool form1 = P.intf_form == 1;
-        uint32_t* const masks = G.nbmask + k;  // [c * n]: this particle's bits of stencil cell c
+        // the forward step's neighbours, recorded by its density pass, as one flat
+        // sequence over the stencil cells (cells of more than 32 particles searched
+        // in place with the forward's test), the lanes of a warp together
+        const uint32_t* const masks = G.nbmask + k;  // [c * n]: this particle's bits of stencil cell c
+        const uint32_t over = masks[(size_t)9 * P.n];
         const Stencil<2> st(P, G.key[k]);
-        const float4 pj4 = G.P4[k];
-        // 1. Candidates by the float test on the cell-relative offsets (a particle
-        // beyond the cutoff's upper guard band is beyond it in double too); a cell
-        // of more than 32 particles is searched in place below.
-        uint32_t over = 0;
-#pragma unroll 1
-        for (int c = 0; c < 9; c++) {
-            uint32_t cand = 0;
-            uint32_t cell;
-            int sx, sy, sz;
-            const uint32_t s = st.cell(c, cell, sx, sy, sz) ? G.cell_start[cell] : kEmpty;
-            const uint32_t e = s != kEmpty ? G.cell_end[cell] : s;
-            if (e - s > 32) {
-                over |= 1u << c;
-            } else {
-                const float shx = (float)sx * P.mf.cell - pj4.x, shy = (float)sy * P.mf.cell - pj4.y;
-                for (uint32_t i = s; i < e; i++) {
-                    const float4 pi4 = G.P4[i];
-                    const float fx = pi4.x + shx, fy = pi4.y + shy;
-                    const bool cnd = i != k && __float_as_int(pi4.w) != P.type_non_existent &&
-                                     fx * fx + fy * fy < P.mf.cut2_hi;
-                    cand |= (cnd ? 1u : 0u) << (i - s);
-                }
-            }
-            masks[(size_t)c * P.n] = cand;
-        }
-        masks[(size_t)9 * P.n] = over;
-        // 2. The candidates as one flat sequence (cells in stencil order, ids
-        // ascending): the forward step's double test, then the pair's adjoint
-        // terms, with the lanes of a warp together; a cell's neighbours replace
-        // its candidates in the masks (the density adjoint reads them).
         int c = -1;
-        uint32_t bits = 0, base = 0, kept = 0;
-        uint32_t next = 0, end = 0;
-        bool masked = false;
+        uint32_t bits = 0, base = 0, next = 0, end = 0;
         for (;;) {
             if (bits == 0 && next == end) {
-                if (masked) masks[(size_t)c * P.n] = kept;
-                masked = false;
                 for (c++; c < 9; c++) {
                     uint32_t cell;
                     int sx, sy, sz;
+                    if (!st.cell(c, cell, sx, sy, sz)) continue;
+                    const uint32_t s = G.cell_start[cell];
+                    if (s == kEmpty) continue;
                     if ((over >> c) & 1u) {
-                        st.cell(c, cell, sx, sy, sz);
-                        next = G.cell_start[cell];
+                        next = s;
                         end = G.cell_end[cell];
                         break;
                     }
                     bits = masks[(size_t)c * P.n];
-                    if (bits) {
-                        st.cell(c, cell, sx, sy, sz);
-                        base = G.cell_start[cell];
-                        kept = 0;
-                        masked = true;
-                        break;
-                    }
+                    base = s;
+                    if (bits) break;
                 }
                 if (c >= 9) break;
             }
-            uint32_t i, b = 0;
-            bool searched;
+            uint32_t i;
+            bool known;
             if (bits) {
-                b = (uint32_t)(__ffs(bits) - 1);
-                i = base + b;
+                i = base + (uint32_t)(__ffs(bits) - 1);
                 bits &= bits - 1;
-                searched = false;
+                known = true;
             } else {
                 i = next++;
-                searched = true;
+                known = false;
             }
             const int32_t ti = G.itype[i];
             const double ex = __dsub_rn(G.rx[i], xj), ey = __dsub_rn(G.ry[i], yj);
             const double s2 = exact_dist2<2>(ex, ey, 0.0);
-            if (!(s2 < P.cut2)) continue;
-            if (searched && (i == k || ti == P.type_non_existent)) continue;
-            kept |= (searched ? 0u : 1u) << b;
+            if (!known && !(i != k && ti != P.type_non_existent && s2 < P.cut2)) continue;
             const double inv_d = rsqrt(s2);
             const double q = s2 * inv_d * P.inv_h;
             double sc, sc1d;
@@ -418,6 +381,9 @@ struct AdjointRun {
     rrsph::Snap ck{}, seg{};
     rrsph::StepScalars* ck_scal = nullptr;  // [nck]
     double* seg_rho = nullptr;
+    // the segment's forward grids: sorted keys and ids, and the neighbour masks
+    // of each step's density pass ([K][n], [K][n], [K][10][n])
+    uint32_t *seg_key = nullptr, *seg_id = nullptr, *seg_mask = nullptr;
     double* lam[2][6] = {};
     double *la_x = nullptr, *la_y = nullptr, *lrho = nullptr, *pr2 = nullptr, *gvx = nullptr;
     double* g_steps = nullptr;
@@ -559,12 +525,13 @@ void enqueue_reverse_step(rrsph_solver* s, AdjointRun* run, uint64_t m, size_t j
     cudaStream_t st = s->stream;
     rrsph::SnapView sv{run->seg.rx + j * n, run->seg.ry + j * n, run->seg.vx + j * n, run->seg.vy + j * n,
                        run->seg.ax + j * n, run->seg.ay + j * n, run->seg.itype + j * n};
-    rrsph::State Sv = s->S;
-    Sv.rx = const_cast<double*>(sv.rx);
-    Sv.ry = const_cast<double*>(sv.ry);
-    rrsph::launch_keys<2>(s->P, Sv, s->G, s->scal, 0, s->flags, st);
-    rrsph::radix_sort_pairs(s->G.keys_in, s->G.ids_in, s->G.keys_a, s->G.ids_a, s->G.sort_scratch, s->P.n,
-                            s->sort_bits, st, &s->G.key, &s->G.id, &s->launches);
+    // the forward step's grid and neighbour masks (recorded in the recompute);
+    // the cell table is rebuilt from the recorded keys, from empty
+    rrsph::Sorted G = s->G;
+    G.key = run->seg_key + j * n;
+    G.id = run->seg_id + j * n;
+    G.nbmask = run->seg_mask + j * 10 * n;
+    rrsph::launch_clear_cells(G.cell_start, s->P.max_cells, st);
     const int nxt = cur ^ 1;
     rrsph::AdjBuf A{run->lam[cur][0], run->lam[cur][1], run->lam[cur][2], run->lam[cur][3], run->lam[cur][4],
                     run->lam[cur][5], run->lam[nxt][0], run->lam[nxt][1], run->lam[nxt][2], run->lam[nxt][3],
@@ -574,10 +541,9 @@ void enqueue_reverse_step(rrsph_solver* s, AdjointRun* run, uint64_t m, size_t j
     const double v_dt = (run->step0 + m) ? run->dt : run->dt * 0.5;
     const unsigned blocks = (unsigned)((n + 255) / 256);
     const unsigned gblocks = (unsigned)((n + rrsph::kAdjThreads - 1) / rrsph::kAdjThreads);
-    rrsph::k_adj_reorder<<<blocks, 256, 0, st>>>(s->P, s->G, sv, run->seg_rho + j * n, s->S.coff2, A, run->dt, v_dt,
-                                                 piston);
-    rrsph::k_adj_forces<<<gblocks, rrsph::kAdjThreads, 0, st>>>(s->P, s->G, A, run->dt);
-    rrsph::k_adj_density<<<gblocks, rrsph::kAdjThreads, 0, st>>>(s->P, s->G, A);
+    rrsph::k_adj_reorder<<<blocks, 256, 0, st>>>(s->P, G, sv, run->seg_rho + j * n, A, run->dt, v_dt, piston);
+    rrsph::k_adj_forces<<<gblocks, rrsph::kAdjThreads, 0, st>>>(s->P, G, A, run->dt);
+    rrsph::k_adj_density<<<gblocks, rrsph::kAdjThreads, 0, st>>>(s->P, G, A);
     s->launches += 4;
     if (piston) {
         rrsph::k_adj_piston_sum<<<1, 256, 0, st>>>(run->gvx, s->P.nwm_start, s->P.nwm_end, run->g_steps + m);
@@ -635,7 +601,9 @@ extern "C" int rrsph_adjoint_forward(rrsph_solver* s, const rrsph_adjoint_config
     std::memcpy(run->fourier_coef, s->P.fourier_coef, sizeof(run->fourier_coef));
     const size_t n = s->P.n;
     if ((rc = alloc_snap(run, run->ck, run->nck, n)) != 0 || (rc = alloc_snap(run, run->seg, run->K, n)) != 0 ||
-        (rc = adj_alloc(run, &run->ck_scal, run->nck)) != 0 || (rc = adj_alloc(run, &run->seg_rho, run->K * n)) != 0)
+        (rc = adj_alloc(run, &run->ck_scal, run->nck)) != 0 || (rc = adj_alloc(run, &run->seg_rho, run->K * n)) != 0 ||
+        (rc = adj_alloc(run, &run->seg_key, run->K * n)) != 0 || (rc = adj_alloc(run, &run->seg_id, run->K * n)) != 0 ||
+        (rc = adj_alloc(run, &run->seg_mask, run->K * 10 * n)) != 0)
         return rc;
     for (auto& set : run->lam)
         for (auto& p : set)
@@ -733,12 +701,22 @@ extern "C" int rrsph_adjoint_reverse(rrsph_solver* s, const double* dgauges, dou
             if ((rc = rrsph_step_async(s, 1)) != 0) return rc;
             ADJ_TRY(cudaMemcpyAsync(run->seg_rho + (m - m0) * n, s->S.rho, n * sizeof(double),
                                     cudaMemcpyDeviceToDevice, st));
+            ADJ_TRY(cudaMemcpyAsync(run->seg_key + (m - m0) * n, s->G.key, n * sizeof(uint32_t),
+                                    cudaMemcpyDeviceToDevice, st));
+            ADJ_TRY(cudaMemcpyAsync(run->seg_id + (m - m0) * n, s->G.id, n * sizeof(uint32_t),
+                                    cudaMemcpyDeviceToDevice, st));
+            ADJ_TRY(cudaMemcpyAsync(run->seg_mask + (m - m0) * 10 * n, s->G.nbmask, 10 * n * sizeof(uint32_t),
+                                    cudaMemcpyDeviceToDevice, st));
         }
         for (uint64_t m = m1; m-- > m0;) {
             enqueue_reverse_step(s, run, m, m - m0, cur);
             cur ^= 1;
             enqueue_seed(s, run, m, cur, dgauges);
         }
+        // the forward steps' key passes clear only the cells they filled: leave
+        // no cell of the reversed grids behind
+        rrsph::launch_clear_cells(s->G.cell_start, s->P.max_cells, st);
+        s->launches++;
     }
     if ((rc = checkpoint_restore(s, run, run->nck - 1, run->N)) != 0) return rc;
     ADJ_TRY(cudaMemcpyAsync(s->S.rho, run->end_rho, n * sizeof(double), cudaMemcpyDeviceToDevice, st));

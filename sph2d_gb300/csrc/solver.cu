@@ -202,13 +202,22 @@ int check_handle(rrsph_solver* s, const char* fn) {
     return RRSPH_OK;
 }
 
+// The stable sort of the key pass's (cell, id) pairs into (keys_a, ids_a),
+// whatever the number of passes: the grid stays there after the step, while
+// the whole step's key pass rewrites (keys_in, ids_in) for the next one.
+void sort_grid(rrsph_solver* s, cudaStream_t st) {
+    rrsph::radix_sort_pairs_into(s->G.keys_in, s->G.ids_in, s->G.keys_a, s->G.ids_a, s->G.keys_b, s->G.ids_b,
+                                 s->G.sort_scratch, s->P.n, s->sort_bits, st, &s->launches);
+    s->G.key = s->G.keys_a;
+    s->G.id = s->G.ids_a;
+}
+
 // Builds the grid on the current state: keys (optionally with the predictor),
 // sort, reorder with the given force-side sources.
 template <int DIM>
 void enqueue_grid(rrsph_solver* s, int predict, rrsph::StepScalars* scal, rrsph::GatherSrc fsrc) {
     rrsph::launch_keys<DIM>(s->P, s->S, s->G, scal, predict, s->flags, s->stream);
-    rrsph::radix_sort_pairs(s->G.keys_in, s->G.ids_in, s->G.keys_a, s->G.ids_a, s->G.sort_scratch, s->P.n,
-                            s->sort_bits, s->stream, &s->G.key, &s->G.id, &s->launches);
+    sort_grid(s, s->stream);
     rrsph::launch_reorder<DIM>(s->P, s->S, s->G, fsrc, s->precision == RRSPH_PRECISION_MIXED, s->stream);
     s->launches += 2;
 }
@@ -389,8 +398,7 @@ void enqueue_step(rrsph_solver* s, int par, cudaEvent_t* events, bool with_keys)
         s->launches++;
     }
     if (events) cudaEventRecord(events[1], s->stream);
-    rrsph::radix_sort_pairs(s->G.keys_in, s->G.ids_in, s->G.keys_a, s->G.ids_a, s->G.sort_scratch, s->P.n,
-                            s->sort_bits, s->stream, &s->G.key, &s->G.id, &s->launches);
+    sort_grid(s, s->stream);
     if (events) cudaEventRecord(events[2], s->stream);
     rrsph::launch_reorder<DIM>(s->P, s->S, s->G, fsrc, s->precision == RRSPH_PRECISION_MIXED, s->stream);
     if (events) cudaEventRecord(events[3], s->stream);
@@ -495,7 +503,7 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
     if (p->average_velocity) { A(S.avx, n); A(S.avy, n); if (d3) A(S.avz, n); }
     A(S.rho, n); A(S.p, n); A(S.drho, n); A(S.rho_pred, n); A(S.mu, n);
     A(S.itype, n); A(S.key_of, n);
-    A(G.keys_in, n); A(G.ids_in, n); A(G.keys_a, n); A(G.ids_a, n);
+    A(G.keys_in, n); A(G.ids_in, n); A(G.keys_a, n); A(G.ids_a, n); A(G.keys_b, n); A(G.ids_b, n);
     A(G.sort_scratch, rrsph::sort_scratch_words((uint32_t)n));
     A(G.cell_start, (size_t)s->P.max_cells); A(G.cell_end, (size_t)s->P.max_cells);
     A(G.rx, n); A(G.ry, n); if (d3) A(G.rz, n);
@@ -522,7 +530,6 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
             }
             S.vl_gone = S.vl_rebuild + 1;
             A(G.vlist, cap * n); A(G.vcount, n); A(G.nlist, cap * n); A(G.ncount, n);
-            A(G.keys_b, n); A(G.ids_b, n);
         }
         A(G.P4, n); A(G.V4, n); A(G.PR, n);
         if (cont) A(G.VD4, n);

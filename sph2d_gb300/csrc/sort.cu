@@ -143,27 +143,6 @@ __global__ void __launch_bounds__(kSortThreads) k_scatter(const uint32_t* __rest
 
 }  // namespace
 
-void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, uint32_t* scratch,
-                      uint32_t n, int bits, cudaStream_t stream, uint32_t** keys_out, uint32_t** vals_out,
-                      unsigned long long* launches) {
-    const uint32_t tiles = sort_tiles(n);
-    uint32_t* counts = scratch;
-    uint32_t* totals = scratch + (size_t)kRadix * tiles;
-    uint32_t *ki = keys, *vi = vals, *ko = keys_alt, *vo = vals_alt;
-    if (n > 0) {
-        for (int shift = 0; shift < bits; shift += 8) {
-            k_tile_hist<<<tiles, kSortThreads, 0, stream>>>(ki, n, shift, tiles, counts);
-            k_digit_scan<<<kRadix * 32 / 256, 256, 0, stream>>>(counts, tiles, totals);
-            k_scatter<<<tiles, kSortThreads, 0, stream>>>(ki, vi, ko, vo, n, shift, tiles, counts, totals);
-            if (launches) *launches += 3;
-            uint32_t* t = ki; ki = ko; ko = t;
-            t = vi; vi = vo; vo = t;
-        }
-    }
-    *keys_out = ki;
-    *vals_out = vi;
-}
-
 void radix_sort_pairs_into(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
                            uint32_t* keys_tmp, uint32_t* vals_tmp, uint32_t* counts, uint32_t n, int bits,
                            cudaStream_t stream, unsigned long long* launches) {

@@ -16,17 +16,10 @@ inline uint32_t sort_tiles(uint32_t n) { return (n + kSortTile - 1) / kSortTile;
 inline size_t sort_scratch_words(uint32_t n) { return (size_t)kRadix * sort_tiles(n) + kRadix; }
 
 // Sorts n pairs by the low `bits` bits of the keys, stably (equal keys keep
-// their input order). keys/vals hold the input; keys_alt/vals_alt are equal
-// sized buffers. On return *keys_out/*vals_out point at whichever pair of
-// buffers holds the result. scratch holds sort_scratch_words(n) words.
-// Launches 3 kernels per 8-bit digit on `stream`; adds them to *launches.
-void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt,
-                      uint32_t* scratch, uint32_t n, int bits, cudaStream_t stream,
-                      uint32_t** keys_out, uint32_t** vals_out, unsigned long long* launches);
-
-// Same sort with caller-given buffers: reads keys_in/vals_in (not modified),
-// leaves the result in keys_out/vals_out, and uses keys_tmp/vals_tmp (n words
-// each) and counts (sort_scratch_words(n) words) as working memory.
+// their input order): reads keys_in/vals_in (not modified), leaves the result
+// in keys_out/vals_out, and uses keys_tmp/vals_tmp (n words each) and counts
+// (sort_scratch_words(n) words) as working memory. Launches 3 kernels per
+// 8-bit digit on `stream`; adds them to *launches.
 void radix_sort_pairs_into(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
                            uint32_t* keys_tmp, uint32_t* vals_tmp, uint32_t* counts, uint32_t n, int bits,
                            cudaStream_t stream, unsigned long long* launches);
