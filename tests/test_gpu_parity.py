@@ -809,6 +809,54 @@ def test_step_host_equals_upload_step_download(gpu_available, precision, treatme
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_step_host_3d_padded_arrays(gpu_available, precision):
+    """rrsph_step_host on the reference's 3D layout (rr_float3: four doubles,
+    the fourth a pad) in page-locked memory, against upload + step + download
+    of the same padded arrays; the pad comes back zero."""
+    import ctypes as C
+
+    import torch
+
+    from sph2d_gb300 import Solver, capi, cases
+    from sph2d_gb300.capi import lib
+
+    case = cases.dam_break_3d(dx=0.02)
+    p = case.params()
+    n = case.ntotal
+
+    def padded(a):
+        out = np.zeros((n, 4))
+        out[:, :3] = a
+        return out
+
+    def dp(a):
+        return a.ctypes.data_as(C.POINTER(C.c_double))
+
+    with Solver(p, precision) as s:
+        r4, v4 = padded(case.r), padded(case.v)
+        rho, it = case.rho.copy(), case.itype.astype(np.int32)
+        capi.check(lib().rrsph_upload(s.handle, dp(r4), 4, dp(v4), dp(rho), None,
+                                      it.ctypes.data_as(C.POINTER(C.c_int32))))
+        t = s.step(12, 0.0)
+        pres = np.zeros(n)
+        capi.check(lib().rrsph_download(s.handle, dp(r4), 4, dp(v4), dp(rho), dp(pres),
+                                        it.ctypes.data_as(C.POINTER(C.c_int32))))
+        ref = {"r": r4, "v": v4, "rho": rho, "p": pres, "itype": it, "t": t}
+
+    def pin(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+
+    h = {"r": pin(padded(case.r)), "v": pin(padded(case.v)), "rho": pin(case.rho),
+         "itype": pin(case.itype.astype(np.int32)), "p": pin(np.zeros(n))}
+    with Solver(p, precision) as s:
+        t = s.step_host(h, 12, 0.0)
+    assert t == ref["t"]
+    for k in ("r", "v", "rho", "p", "itype"):
+        assert np.array_equal(h[k], ref[k]), k
+    assert not h["r"][:, 3].any() and not h["v"][:, 3].any()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("treatment", [0, 1])
 def test_step_download_equals_step_then_download(gpu_available, precision, treatment):
     """rrsph_step_download (the state staying on the device) against rrsph_step
