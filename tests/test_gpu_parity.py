@@ -882,6 +882,38 @@ def test_step_download_equals_step_then_download(gpu_available, precision, treat
                 assert np.array_equal(st[k], ref[j][1][k]), (j, k)
 
 
+def test_step_host_and_step_download_check_their_arguments(gpu_available):
+    import ctypes as C
+
+    from sph2d_gb300 import Solver, capi
+    from sph2d_gb300.capi import lib
+
+    case = _dam(nx=10, ny=10)
+    p = case.params()
+    n = case.ntotal
+    r, v, rho, pres = np.zeros((n, 2)), np.zeros((n, 2)), np.zeros(n), np.zeros(n)
+    it = np.zeros(n, dtype=np.int32)
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    ip = it.ctypes.data_as(C.POINTER(C.c_int32))
+    t = C.c_double(0.0)
+    with Solver(p, "mixed") as s:
+        s.upload(case.r, case.v, case.rho, case.itype)
+        h = s.handle
+        bad = [
+            lib().rrsph_step_host(h, 1, C.byref(t), None, 2, dp(v), dp(rho), dp(pres), ip),
+            lib().rrsph_step_host(h, 1, C.byref(t), dp(r), 1, dp(v), dp(rho), dp(pres), ip),
+            lib().rrsph_step_host(h, 0, C.byref(t), dp(r), 2, dp(v), dp(rho), dp(pres), ip),
+            lib().rrsph_step_host(h, 1, None, dp(r), 2, dp(v), dp(rho), dp(pres), ip),
+            lib().rrsph_step_download(h, 1, None, dp(r), 2, dp(v), dp(rho), dp(pres), ip),
+            lib().rrsph_step_download(h, 1, C.byref(t), dp(r), 1, dp(v), dp(rho), dp(pres), ip),
+            lib().rrsph_step_download(h, 0, C.byref(t), dp(r), 2, dp(v), dp(rho), dp(pres), ip),
+        ]
+        assert all(rc == capi.ERR_INVALID_ARGUMENT for rc in bad), bad
+        # nothing stepped: the solver still runs, and a download of a subset works
+        assert lib().rrsph_step_download(h, 2, C.byref(t), None, 2, None, dp(rho), None, None) == 0
+        assert t.value > 0 and rho.min() > 0
+
+
 def test_pinned_host_arrays_upload_and_download_directly(gpu_available):
     """Page-locked caller arrays go through one kernel each way (read and
     written over the host link); the state equals that of pageable arrays,
