@@ -232,3 +232,30 @@ def test_empty_particle_set_is_an_error():
     q = params_from_json(_model(), _particle(ntotal=10, nfluid=11, nvirt=0))
     with pytest.raises(RrsphError, match="bad particle counts"):
         derive(q, np.zeros((10, 2)))
+
+
+def test_readme_c_usage_compiles(tmp_path):
+    """The C usage in README.md compiles against include/rrsph_cuda.h."""
+    import re
+    import shutil
+    import subprocess
+    from pathlib import Path
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    root = Path(__file__).resolve().parent.parent
+    block = re.search(r"```c\n(.*?)```", (root / "README.md").read_text(), re.S)
+    assert block, "no C block in README.md"
+    src = tmp_path / "usage.c"
+    src.write_text(
+        '#include <stdint.h>\n#include "rrsph_cuda.h"\n'
+        "int main(void) {\n"
+        "    static double r[2], v[2], rho[1], pres[1];\n"
+        "    static int32_t itype[1];\n"
+        + block.group(1)
+        + "    return 0;\n}\n"
+    )
+    res = subprocess.run([cc, "-std=c11", "-Wall", "-Werror", "-c", str(src), "-I", str(root / "include"),
+                          "-o", str(tmp_path / "usage.o")], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
