@@ -348,7 +348,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     e2e_time = [0.0]
 
     def e2e_step():
-        # r, v, rho, itype in and out; p out only (the density pass computes it from rho), as in the reference's loop
+        # r, v, rho, itype in and out (rho read only with continuity density); p out only, as in the reference's loop
         tt = C.c_double(e2e_time[0])
         capi.check(L.rrsph_step_host(sm.handle, 1, C.byref(tt), dp(host["r"]), 2, dp(host["v"]), dp(host["rho"]),
                                      dp(host["p"]), ip(host["itype"])))
@@ -376,7 +376,8 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     clocks_info = clocks.stop()
     if clocks_info is not None:
         clocks_info["window"] = "from the timed steps to the end of the e2e loop"
-    h2d = n * (2 * 8 + 2 * 8 + 8 + 4)      # r, v, rho, itype
+    # r, v, itype (and rho with continuity density: with summation density the step recomputes it)
+    h2d = n * (2 * 8 + 2 * 8 + 4 + (8 if p.density_treatment else 0))
     d2h = n * (2 * 8 + 2 * 8 + 8 + 8 + 4)  # r, v, rho, p, itype
 
     # ---- aggregate over the replicas (the slowest rank's time, the pairs of all ranks)
@@ -454,9 +455,10 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": e2e_steps, "rebuilds": e2e_rebuilds,
                 "ms_per_step_median": statistics.median(e2e_each) * 1e3, "ms_per_step_max": max(e2e_each) * 1e3,
-                "path": "rrsph_step_host(1) per step on pinned host buffers (upload of r, v, rho, itype, one "
-                        "step, download of r, v, rho, p, itype into the same arrays, one wait), each step "
-                        "uploading the state the last one returned"},
+                "path": "rrsph_step_host(1) per step on pinned host buffers (upload of r, v, itype: the "
+                        "flume's summation density recomputes rho, which the call does not upload; one step; "
+                        "download of r, v, rho, p, itype into the same arrays; one wait), each step uploading "
+                        "the state the last one returned"},
         "gpu_launches": launches,
         "checks": {
             "fluid_mass_exact": diag1["mass"] == diag0["mass"],

@@ -236,7 +236,8 @@ __device__ __forceinline__ void host_write3(double* __restrict__ a, size_t b, bo
 // (thread 0) the step scalars of step 0, then the first step's predict + key
 // pass of k_keys (zero acceleration, dt of step 0) while the link is still
 // busy. The neighbour-list check of an upload runs before this kernel: its
-// key pass may raise the rebuild flag, which the check resets.
+// key pass may raise the rebuild flag, which the check resets. rho may be
+// null with summation density, whose step recomputes it before any read.
 template <int DIM>
 __global__ void k_upload_direct(DevParams P, State S, Sorted G, const double* __restrict__ r,
                                 const double* __restrict__ v, const double* __restrict__ rho,
@@ -261,7 +262,7 @@ __global__ void k_upload_direct(DevParams P, State S, Sorted G, const double* __
         S.vz[i] = z;
         S.az[i] = 0.0;
     }
-    const double rh = rho[i];
+    const double rh = rho ? rho[i] : P.rho0;  // no rho: summation density, which the step recomputes
     S.rho[i] = rh;
     S.p[i] = p ? p[i] : 0.0;
     S.itype[i] = itype[i];

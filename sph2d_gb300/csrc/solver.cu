@@ -645,7 +645,8 @@ const void* device_view(const void* host) {
 int finish_upload(rrsph_solver* s, bool wait);
 
 // rrsph_upload without the checks; wait: return after the caller's arrays
-// were read (else they are read in stream order).
+// were read (else they are read in stream order). rho may be null with
+// summation density (rrsph_step_host: the step recomputes it before any read).
 int upload_impl(rrsph_solver* s, const double* r, uint32_t stride, const double* v, const double* rho,
                 const double* pres, const int32_t* itype, bool wait) {
     int rc;
@@ -658,7 +659,7 @@ int upload_impl(rrsph_solver* s, const double* r, uint32_t stride, const double*
     const double* drho = static_cast<const double*>(device_view(rho));
     const double* dp = static_cast<const double*>(device_view(pres));
     const int32_t* dit = static_cast<const int32_t*>(device_view(itype));
-    if (dr && dv && drho && dit && (dp || !pres)) {
+    if (dr && dv && (drho || !rho) && dit && (dp || !pres)) {
         if (s->verlet) set_verlet_copies(s, 0, 0);  // step 0 reads the copies its key pass writes
         if (S.vl_rebuild) {  // before the key pass below, which may raise the flag again
             rrsph::launch_verlet_upload_check(S.vl_rebuild, S.vl_gone, st);
@@ -683,7 +684,7 @@ int upload_impl(rrsph_solver* s, const double* r, uint32_t stride, const double*
     if (s->dim == 3) rrsph::launch_unpack<3>(s->P, S, s->staging, s->staging + n * stride, stride, st);
     else rrsph::launch_unpack<2>(s->P, S, s->staging, s->staging + n * stride, stride, st);
     s->launches++;
-    RRSPH_CUDA_TRY(cudaMemcpyAsync(S.rho, rho, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (rho) RRSPH_CUDA_TRY(cudaMemcpyAsync(S.rho, rho, n * sizeof(double), cudaMemcpyHostToDevice, st));
     if (pres) RRSPH_CUDA_TRY(cudaMemcpyAsync(S.p, pres, n * sizeof(double), cudaMemcpyHostToDevice, st));
     else RRSPH_CUDA_TRY(cudaMemsetAsync(S.p, 0, n * sizeof(double), st));
     RRSPH_CUDA_TRY(cudaMemcpyAsync(S.itype, itype, n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
@@ -941,7 +942,9 @@ int steps_and_download(rrsph_solver* s, uint64_t nsteps, double* time_io, double
             cudaEventCreateWithFlags(&s->ev_dl, cudaEventDisableTiming) != cudaSuccess)
             return set_error(RRSPH_ERR_CUDA, "rrsph_step_host: copy stream");
     }
-    if (upload && (rc = upload_impl(s, r, stride, v, rho, nullptr, itype, false)) != 0) return rc;
+    // with summation density the step recomputes rho before reading it: not uploaded
+    const double* rho_in = s->P.density_treatment == 0 ? nullptr : rho;
+    if (upload && (rc = upload_impl(s, r, stride, v, rho_in, nullptr, itype, false)) != 0) return rc;
     rrsph::launch_set_time(&s->scal[s->step_index & 1], *time_io, s->flags, st);  // time, flags cleared
     RRSPH_CUDA_TRY(cudaGetLastError());
     s->launches++;
