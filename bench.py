@@ -378,7 +378,10 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         clocks_info["window"] = "from the timed steps to the end of the e2e loop"
     # r, v, itype (and rho with continuity density: with summation density the step recomputes it)
     h2d = n * (2 * 8 + 2 * 8 + 4 + (8 if p.density_treatment else 0))
-    d2h = n * (2 * 8 + 2 * 8 + 8 + 8 + 4)  # r, v, rho, p, itype
+    # r, v, rho, p; itype only when a step can change a type (the consistency fix, the vanishing wall):
+    # rrsph_step_host rewrites its page-locked itype only if a step changed one
+    types_change = p.consistency_treatment == 2 or p.nwm == 4
+    d2h = n * (2 * 8 + 2 * 8 + 8 + 8 + (4 if types_change else 0))
 
     # ---- aggregate over the replicas (the slowest rank's time, the pairs of all ranks)
     t_s, tot_pairs, e2e_max, e2e_all = aggregate_replicas(ms_mixed / 1e3, pairs_timed, e2e_s, e2e_pairs, dist,
@@ -457,8 +460,9 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
                 "ms_per_step_median": statistics.median(e2e_each) * 1e3, "ms_per_step_max": max(e2e_each) * 1e3,
                 "path": "rrsph_step_host(1) per step on pinned host buffers (upload of r, v, itype: the "
                         "flume's summation density recomputes rho, which the call does not upload; one step; "
-                        "download of r, v, rho, p, itype into the same arrays; one wait), each step uploading "
-                        "the state the last one returned"},
+                        "download of r, v, rho, p into the same arrays, and itype when a step changed a type, "
+                        "which the flume's does not; one wait), each step uploading the state the last one "
+                        "returned"},
         "gpu_launches": launches,
         "checks": {
             "fluid_mass_exact": diag1["mass"] == diag0["mass"],

@@ -219,7 +219,8 @@ int rrsph_step(rrsph_solver* s, uint64_t nsteps, double* time_io);
  * on its arrays: rrsph_upload(r, stride, v, rho, NULL, itype), rrsph_step(
  * nsteps, time_io), rrsph_download(r, stride, v, rho, pres, itype), with one
  * wait at the end (rho is not read with summation density, whose first step
- * recomputes it). r, v, rho and itype are read, then overwritten with the
+ * recomputes it; a page-locked itype, read at the upload, is rewritten only if
+ * a step changed a type). r, v, rho and itype are read, then overwritten with the
  * state after the steps; pres (may be NULL) receives p. With graph replay, p
  * (and rho with summation density, which the whole step does not change)
  * come back while the last step's force gather runs. Page-locked arrays are

@@ -34,6 +34,7 @@ struct State {
     float4* boff4;             // 3D: the same (x, y, z)
     uint32_t* vl_rebuild;      // non-zero: the next step rebuilds the grid and the lists
     uint32_t* vl_gone;         // the last build: bit 0 left out non-existent particles, bit 1 overflowed a list
+    uint32_t* itype_changed;   // non-zero once a step changed a particle's type since the last upload
 };
 
 // Per-step cell-ordered copies and the grid.
@@ -179,9 +180,10 @@ template <int DIM>
 void launch_upload_direct(const DevParams& P, const State& S, const Sorted& G, const double* r, const double* v,
                           const double* rho, const double* p, const int32_t* itype, uint32_t stride,
                           StepScalars* scal, double dt, uint32_t* flags, cudaStream_t st);
+// itype_if (optional): itype is written only if that device word is non-zero.
 template <int DIM>
 void launch_download_direct(const DevParams& P, const State& S, double* r, double* v, double* rho, double* p,
-                            int32_t* itype, uint32_t stride, cudaStream_t st);
+                            int32_t* itype, uint32_t stride, cudaStream_t st, const uint32_t* itype_if = nullptr);
 
 // Compile-time variant: the cell-tile density pass of the 2D mixed step with
 // neighbour reuse (summation density, cubic kernel) instead of the

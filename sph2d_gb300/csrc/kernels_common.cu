@@ -358,11 +358,12 @@ __global__ void k_report(const StepScalars* __restrict__ scal, const StepScalars
 }
 
 // rrsph_download into host arrays the device can address: one pass writing
-// the requested arrays (null: skipped) over the host link.
+// the requested arrays (null: skipped) over the host link; itype only if
+// itype_if (when given) is non-zero.
 template <int DIM>
 __global__ void k_download_direct(DevParams P, State S, double* __restrict__ r, double* __restrict__ v,
                                   double* __restrict__ rho, double* __restrict__ p, int32_t* __restrict__ itype,
-                                  uint32_t stride, int vec) {
+                                  uint32_t stride, int vec, const uint32_t* __restrict__ itype_if) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const size_t b = (size_t)i * stride;
@@ -370,7 +371,7 @@ __global__ void k_download_direct(DevParams P, State S, double* __restrict__ r, 
     if (v) host_write3<DIM>(v, b, vec, S.vx[i], S.vy[i], DIM == 3 ? S.vz[i] : 0.0);
     if (rho) rho[i] = S.rho[i];
     if (p) p[i] = S.p[i];
-    if (itype) itype[i] = S.itype[i];
+    if (itype && (!itype_if || *itype_if)) itype[i] = S.itype[i];
 }
 
 }  // namespace
@@ -404,9 +405,9 @@ void launch_upload_direct(const DevParams& P, const State& S, const Sorted& G, c
 }
 template <int DIM>
 void launch_download_direct(const DevParams& P, const State& S, double* r, double* v, double* rho, double* p,
-                            int32_t* itype, uint32_t stride, cudaStream_t st) {
+                            int32_t* itype, uint32_t stride, cudaStream_t st, const uint32_t* itype_if) {
     k_download_direct<DIM><<<blocks_for(P.n, 256), 256, 0, st>>>(P, S, r, v, rho, p, itype, stride,
-                                                                 vec_layout(DIM, stride, r, v));
+                                                                 vec_layout(DIM, stride, r, v), itype_if);
 }
 
 template <int DIM>
@@ -469,7 +470,7 @@ void launch_pack(const DevParams& P, State S, double* r, double* v, uint32_t str
                                           const double*, const double*, const double*, const int32_t*,         \
                                           uint32_t, StepScalars*, double, uint32_t*, cudaStream_t);            \
     template void launch_download_direct<D>(const DevParams&, const State&, double*, double*, double*, double*, \
-                                            int32_t*, uint32_t, cudaStream_t);
+                                            int32_t*, uint32_t, cudaStream_t, const uint32_t*);
 RRSPH_INSTANTIATE(2)
 RRSPH_INSTANTIATE(3)
 #undef RRSPH_INSTANTIATE

@@ -502,7 +502,7 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
     if (d3) { A(S.rz, n); A(S.vz, n); A(S.az, n); A(S.vpz, n); }
     if (p->average_velocity) { A(S.avx, n); A(S.avy, n); if (d3) A(S.avz, n); }
     A(S.rho, n); A(S.p, n); A(S.drho, n); A(S.rho_pred, n); A(S.mu, n);
-    A(S.itype, n); A(S.key_of, n);
+    A(S.itype, n); A(S.key_of, n); A(S.itype_changed, 1);
     A(G.keys_in, n); A(G.ids_in, n); A(G.keys_a, n); A(G.ids_a, n); A(G.keys_b, n); A(G.ids_b, n);
     A(G.sort_scratch, rrsph::sort_scratch_words((uint32_t)n));
     A(G.cell_start, (size_t)s->P.max_cells); A(G.cell_end, (size_t)s->P.max_cells);
@@ -589,7 +589,8 @@ extern "C" int rrsph_create(const rrsph_params* p, int precision, rrsph_solver**
     if (cudaMemsetAsync(G.cell_start, 0xFF, (size_t)s->P.max_cells * sizeof(uint32_t), s->stream) != cudaSuccess ||
         cudaMemsetAsync(S.key_of, 0xFF, n * sizeof(uint32_t), s->stream) != cudaSuccess ||
         cudaMemsetAsync(s->scal, 0, 2 * sizeof(rrsph::StepScalars), s->stream) != cudaSuccess ||
-        cudaMemsetAsync(s->flags, 0, sizeof(uint32_t), s->stream) != cudaSuccess)
+        cudaMemsetAsync(s->flags, 0, sizeof(uint32_t), s->stream) != cudaSuccess ||
+        cudaMemsetAsync(S.itype_changed, 0, sizeof(uint32_t), s->stream) != cudaSuccess)
         return fail(set_error(RRSPH_ERR_CUDA, std::string("rrsph_create: memset failed: ") +
                                                   cudaGetErrorString(cudaGetLastError())));
     for (int i = 0; i <= kPhases; i++) {
@@ -653,6 +654,7 @@ int upload_impl(rrsph_solver* s, const double* r, uint32_t stride, const double*
     const size_t n = s->P.n;
     auto& S = s->S;
     cudaStream_t st = s->stream;
+    RRSPH_CUDA_TRY(cudaMemsetAsync(S.itype_changed, 0, sizeof(uint32_t), st));  // the uploaded types are the reference
     // page-locked caller arrays: one kernel reads them over the host link
     const double* dr = static_cast<const double*>(device_view(r));
     const double* dv = static_cast<const double*>(device_view(v));
@@ -734,9 +736,11 @@ int finish_upload(rrsph_solver* s, bool wait) {
 }  // namespace
 
 namespace {
-// rrsph_download without the checks; wait: return after the arrays were written.
+// rrsph_download without the checks; wait: return after the arrays were written;
+// itype_if_changed: page-locked itype holds the uploaded types (rrsph_step_host),
+// so it is rewritten only if a step changed a type since.
 int download_impl(rrsph_solver* s, double* r, uint32_t stride, double* v, double* rho, double* pres, int32_t* itype,
-                  bool wait) {
+                  bool wait, bool itype_if_changed = false) {
     int rc;
     const size_t n = s->P.n;
     cudaStream_t st = s->stream;
@@ -747,8 +751,9 @@ int download_impl(rrsph_solver* s, double* r, uint32_t stride, double* v, double
     double* dp = const_cast<double*>(static_cast<const double*>(device_view(pres)));
     int32_t* dit = const_cast<int32_t*>(static_cast<const int32_t*>(device_view(itype)));
     if ((dr || !r) && (dv || !v) && (drho || !rho) && (dp || !pres) && (dit || !itype)) {
-        if (s->dim == 3) rrsph::launch_download_direct<3>(s->P, s->S, dr, dv, drho, dp, dit, stride, st);
-        else rrsph::launch_download_direct<2>(s->P, s->S, dr, dv, drho, dp, dit, stride, st);
+        const uint32_t* itype_if = itype_if_changed ? s->S.itype_changed : nullptr;
+        if (s->dim == 3) rrsph::launch_download_direct<3>(s->P, s->S, dr, dv, drho, dp, dit, stride, st, itype_if);
+        else rrsph::launch_download_direct<2>(s->P, s->S, dr, dv, drho, dp, dit, stride, st, itype_if);
         s->launches++;
         if (wait) RRSPH_CUDA_TRY(cudaStreamSynchronize(st));
         return RRSPH_OK;
@@ -957,7 +962,7 @@ int steps_and_download(rrsph_solver* s, uint64_t nsteps, double* time_io, double
             RRSPH_CUDA_TRY(cudaMemcpyAsync(rho, s->S.rho, n * sizeof(double), cudaMemcpyDeviceToHost, s->dl_stream));
         RRSPH_CUDA_TRY(cudaEventRecord(s->ev_dl, s->dl_stream));
     }
-    if ((rc = download_impl(s, r, stride, v, early_rho ? nullptr : rho, mark ? nullptr : pres, itype, false)) != 0)
+    if ((rc = download_impl(s, r, stride, v, early_rho ? nullptr : rho, mark ? nullptr : pres, itype, false, upload)) != 0)
         return rc;
     if (mark) RRSPH_CUDA_TRY(cudaStreamWaitEvent(st, s->ev_dl, 0));
     return rrsph_sync(s, time_io);

@@ -271,6 +271,7 @@ __device__ __forceinline__ void whole_particle(const DevParams& P, const State& 
             S.vx[i] = vx;
         } else if (P.nwm == 4) {
             S.itype[i] = P.type_non_existent;
+            atomicOr(S.itype_changed, 1u);
         }
     }
     const double v_dt = scal->step ? dt : dhalf(dt);
@@ -303,6 +304,7 @@ __device__ __forceinline__ void whole_particle(const DevParams& P, const State& 
                 move = false;
                 in_known = false;
                 S.itype[i] = P.type_non_existent;
+                atomicOr(S.itype_changed, 1u);
             }
         }
         if (move) {

@@ -882,6 +882,46 @@ def test_step_download_equals_step_then_download(gpu_available, precision, treat
                 assert np.array_equal(st[k], ref[j][1][k]), (j, k)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_step_host_writes_changed_types_back(gpu_available, precision):
+    """With CONSISTENCY_FIX a particle that leaves the geometry becomes
+    non-existent: rrsph_step_host writes the changed types back into its
+    page-locked itype (which it rewrites only when a step changed a type), as
+    upload + step + download does; a further call that changes no type keeps
+    them."""
+    import torch
+
+    from sph2d_gb300 import Solver
+
+    case = _dam(nx=20, ny=10)
+    q = case.params()
+    q.consistency_treatment = 2
+    v = case.v.copy()
+    v[0] = [0.0, -1.0e4]  # leaves the geometry box in one step
+    ref = []
+    with Solver(q, precision) as s:
+        st = {"r": case.r, "v": v, "rho": case.rho, "itype": case.itype}
+        t = 0.0
+        for n in (2, 3):
+            s.upload(st["r"], st["v"], st["rho"], st["itype"])
+            t = s.step(n, t)
+            st = s.download()
+            ref.append(st)
+    assert ref[0]["itype"][0] == 0 and ref[1]["itype"][0] == 0
+
+    def pin(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+
+    h = {"r": pin(case.r), "v": pin(v), "rho": pin(case.rho), "itype": pin(case.itype.astype(np.int32)),
+         "p": pin(np.zeros(case.ntotal))}
+    with Solver(q, precision) as s:
+        t = 0.0
+        for j, n in enumerate((2, 3)):
+            t = s.step_host(h, n, t)
+            for k in ("r", "v", "rho", "p", "itype"):
+                assert np.array_equal(h[k], ref[j][k]), (j, k)
+
+
 def test_step_host_and_step_download_check_their_arguments(gpu_available):
     import ctypes as C
 
