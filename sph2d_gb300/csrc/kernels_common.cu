@@ -247,6 +247,7 @@ __global__ void k_upload_direct(DevParams P, State S, Sorted G, const double* __
     if (i == 0) {
         *scal = StepScalars{};
         scal->dt = dt;
+        *S.itype_changed = 0u;  // the uploaded types are the reference
     }
     if (i >= P.n) return;
     const size_t b = (size_t)i * stride;

@@ -654,8 +654,8 @@ int upload_impl(rrsph_solver* s, const double* r, uint32_t stride, const double*
     const size_t n = s->P.n;
     auto& S = s->S;
     cudaStream_t st = s->stream;
-    RRSPH_CUDA_TRY(cudaMemsetAsync(S.itype_changed, 0, sizeof(uint32_t), st));  // the uploaded types are the reference
-    // page-locked caller arrays: one kernel reads them over the host link
+    // page-locked caller arrays: one kernel reads them over the host link (and
+    // clears itype_changed: the uploaded types are the reference)
     const double* dr = static_cast<const double*>(device_view(r));
     const double* dv = static_cast<const double*>(device_view(v));
     const double* drho = static_cast<const double*>(device_view(rho));
@@ -681,6 +681,7 @@ int upload_impl(rrsph_solver* s, const double* r, uint32_t stride, const double*
         return RRSPH_OK;
     }
     if ((rc = ensure_staging(s, 2 * n * stride)) != 0) return rc;
+    RRSPH_CUDA_TRY(cudaMemsetAsync(S.itype_changed, 0, sizeof(uint32_t), st));  // the uploaded types are the reference
     RRSPH_CUDA_TRY(cudaMemcpyAsync(s->staging, r, n * stride * sizeof(double), cudaMemcpyHostToDevice, st));
     RRSPH_CUDA_TRY(cudaMemcpyAsync(s->staging + n * stride, v, n * stride * sizeof(double), cudaMemcpyHostToDevice, st));
     if (s->dim == 3) rrsph::launch_unpack<3>(s->P, S, s->staging, s->staging + n * stride, stride, st);
